@@ -1,0 +1,81 @@
+"""Loader for libdplr_gb300.so (the CUDA library behind the C ABI).
+
+There is no fallback: if the library is missing or cannot be loaded, every
+entry point raises, so a GPU run can never silently use another path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char, c_double, c_int, c_longlong, c_void_p
+
+from .capi import PlrApi
+from .tree import PDPlrMtx, c_double_p
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libdplr_gb300.so")
+
+_lib = None
+_api = None
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def _bind(lib: ctypes.CDLL) -> None:
+    def sig(name, res, args):
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+
+    sig("dplr_gpu_last_error", ctypes.c_char_p, [])
+    sig("dplr_gpu_plan_create", c_int, [c_int, PDPlrMtx, c_void_p, POINTER(c_void_p)])
+    sig("dplr_gpu_plan_destroy", None, [c_void_p])
+    sig("dplr_gpu_plan_refresh", c_int, [c_void_p, PDPlrMtx, c_void_p])
+    sig("dplr_gpu_plan_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_longlong),
+                                      POINTER(c_int), POINTER(c_int)])
+    sig("dplr_gpu_plan_device_bytes", c_longlong, [c_void_p])
+    sig("dplr_gpu_apply", c_int, [c_void_p, c_char, c_int, c_double, c_void_p, c_int, c_double,
+                                  c_void_p, c_int, c_void_p])
+    sig("dplr_gpu_register", c_int, [c_int, PDPlrMtx])
+    sig("dplr_gpu_unregister", c_int, [PDPlrMtx])
+    for name, res, args in _OPTIONAL:
+        if hasattr(lib, name):
+            sig(name, res, args)
+
+
+# Entry points added by later modules of the library (bound when present).
+_OPTIONAL: list = []
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        try:
+            _lib = ctypes.CDLL(LIB_PATH)
+        except OSError as e:
+            raise NativeError(f"cannot load {LIB_PATH}: {e}") from e
+        _bind(_lib)
+    return _lib
+
+
+def api() -> PlrApi:
+    """The drop-in DPLR entry points (dplrgepmv, dplrgepdmm, ...)."""
+    global _api
+    if _api is None:
+        _api = PlrApi(lib(), "dplr")
+    return _api
+
+
+def last_error() -> str:
+    return lib().dplr_gpu_last_error().decode()
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise NativeError(f"{what} failed ({rc}): {last_error()}")
+
+
+__all__ = ["lib", "api", "last_error", "check", "NativeError", "LIB_PATH", "c_double_p"]

@@ -1,0 +1,380 @@
+// plan.cu -- flatten a host PLR tree into the device block table.
+//
+// The tree walk visits nodes in the order of DPLR's recursions
+// (src/dplrpmv.c:166-173: ne, sw, then nw, se), records one LRDesc per
+// low-rank block and one LeafDesc per dense leaf, assigns every factor
+// array a 256-byte aligned slot in one FP64 pool, and builds the apply
+// schedules for op N and op T.
+#include "internal.cuh"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+
+namespace dg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+const char *last_error_c() { return g_last_error.c_str(); }
+
+static long long align32(long long x) { return (x + 31) & ~31LL; }
+
+// Structural checks performed by DPLR's recursions before they touch any
+// output (src/dplrpmv.c:22-36, :116-130); here they run over the whole
+// tree up front so that a malformed tree never produces partial output.
+static int check_node(const DPlrMtx *A, int m, const char *fn, int depth)
+{
+    if (!A) return fail(DPLR_GPU_EINVAL, "%s: null node", fn);
+    if (depth > 60) return fail(DPLR_GPU_EINVAL, "%s: tree too deep", fn);
+    if (A->type != PLR_DMTX && A->type != PLR_HMTX)
+        return fail(DPLR_GPU_EINVAL, "%s: invalid A type", fn);
+    if (A->size != m) return fail(DPLR_GPU_EINVAL, "%s: invalid A size", fn);
+    if (A->type == PLR_DMTX) {
+        if (m > 0 && !A->dd.d) return fail(DPLR_GPU_EINVAL, "%s: dense leaf without data", fn);
+        if ((long long)m * m > (1LL << 31))
+            return fail(DPLR_GPU_EINVAL, "%s: dense leaf too large", fn);
+        return 0;
+    }
+    if (m % 2 != 0) return fail(DPLR_GPU_EINVAL, "%s: H node of odd size %d", fn, m);
+    int h = m / 2;
+    const DPlrMtx *lr[2] = {A->dh.ne, A->dh.sw};
+    for (const DPlrMtx *L : lr) {
+        if (!L) return fail(DPLR_GPU_EINVAL, "%s: null low-rank block", fn);
+        if (L->type != PLR_LRMTX) return fail(DPLR_GPU_EINVAL, "%s: invalid A type", fn);
+        if (L->size != h) return fail(DPLR_GPU_EINVAL, "%s: invalid A size", fn);
+        if (L->dlr.rank < 0 || L->dlr.rank > L->dlr.capacity)
+            return fail(DPLR_GPU_EINVAL, "%s: rank %d outside [0, capacity %d]", fn,
+                        L->dlr.rank, L->dlr.capacity);
+        if (L->dlr.rank > 0 && (!L->dlr.u || !L->dlr.v || !L->dlr.sig))
+            return fail(DPLR_GPU_EINVAL, "%s: low-rank block without data", fn);
+    }
+    int rc = check_node(A->dh.nw, h, fn, depth + 1);
+    if (rc) return rc;
+    return check_node(A->dh.se, h, fn, depth + 1);
+}
+
+int validate_tree(int m, const DPlrMtx *A, const char *fn)
+{
+    if (m < 0) return fail(DPLR_GPU_EINVAL, "%s: invalid matrix size %d", fn, m);
+    return check_node(A, m, fn, 0);
+}
+
+// ------------------------------------------------------------- flattening
+struct Builder {
+    Plan *p;
+    int walk(const DPlrMtx *A, int row0, int level)
+    {
+        if (A->type == PLR_DMTX) {
+            LeafDesc L;
+            L.d = p->pool_doubles;
+            L.row0 = row0;
+            L.b = A->size;
+            p->pool_doubles += align32((long long)L.b * L.b);
+            p->leaves.push_back(L);
+            p->nnz += (long long)L.b * L.b;
+            return ~(int)(p->leaves.size() - 1);
+        }
+        int idx = (int)p->nodes.size();
+        p->nodes.push_back(HDesc{});
+        int h = A->size / 2;
+        p->levels = std::max(p->levels, level + 1);
+        int ids[2];
+        for (int s = 0; s < 2; ++s) {
+            const DPlrMtx *B = s == 0 ? A->dh.ne : A->dh.sw;
+            LRDesc d;
+            d.n = h;
+            d.rank = B->dlr.rank;
+            d.row0 = s == 0 ? row0 : row0 + h;
+            d.col0 = s == 0 ? row0 + h : row0;
+            d.level = level;
+            d.node = idx;
+            d.is_ne = s == 0;
+            d.u = p->pool_doubles;
+            p->pool_doubles += align32((long long)h * d.rank);
+            d.v = p->pool_doubles;
+            p->pool_doubles += align32((long long)h * d.rank);
+            d.sig = p->pool_doubles;
+            p->pool_doubles += align32(d.rank);
+            d.toff = p->total_rank;
+            p->total_rank += d.rank;
+            p->max_rank = std::max(p->max_rank, d.rank);
+            p->nnz += (long long)h * d.rank;
+            ids[s] = (int)p->lr.size();
+            p->lr.push_back(d);
+        }
+        HDesc hd;
+        hd.row0 = row0;
+        hd.m = A->size;
+        hd.level = level;
+        hd.ne = ids[0];
+        hd.sw = ids[1];
+        hd.parent = -1;
+        hd.nw = walk(A->dh.nw, row0, level + 1);
+        hd.se = walk(A->dh.se, row0 + h, level + 1);
+        if (hd.nw >= 0) p->nodes[hd.nw].parent = idx;
+        if (hd.se >= 0) p->nodes[hd.se].parent = idx;
+        p->nodes[idx] = hd;
+        return idx;
+    }
+};
+
+static int gcd_int(int a, int b) { return b == 0 ? a : gcd_int(b, a % b); }
+
+static void build_schedule(Plan *p, int trans, Schedule &S)
+{
+    const int CH = p->chunk_rows;
+    S.items.clear();
+    S.chunks_of.assign(p->lr.size(), 0);
+    S.poff.assign(p->lr.size(), 0);
+    long long poff = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        S.poff[b] = poff;
+        if (L.rank == 0 || L.n == 0) continue;
+        int nch = (L.n + CH - 1) / CH;
+        S.chunks_of[b] = nch;
+        for (int c = 0; c < nch; ++c) {
+            PanelItem it;
+            it.blk = (int)b;
+            it.r0 = c * CH;
+            it.len = std::min(CH, L.n - c * CH);
+            it.chunk = c;
+            S.items.push_back(it);
+        }
+        poff += (long long)nch * L.rank;
+    }
+    S.partial_per_rhs = poff;
+
+    // Tile height: a power of two (<= 64) dividing every leaf size, so every
+    // block and leaf boundary falls on a tile boundary.
+    int g = 0;
+    for (const LeafDesc &L : p->leaves) g = gcd_int(g, L.b);
+    int R = 64;
+    while (R > 1 && (g % R) != 0) R >>= 1;
+    S.tile_rows = R;
+    int ntiles = p->m / R;
+    std::vector<std::vector<TileTerm>> per(ntiles);
+    // Low-rank terms: the block's output rows are U's rows (op N) or V's (op T).
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        int out0 = trans ? L.col0 : L.row0;
+        long long base = trans ? L.v : L.u;
+        for (int t0 = out0; t0 < out0 + L.n; t0 += R) {
+            TileTerm tt;
+            tt.a = base + (t0 - out0);
+            tt.lda = L.n;
+            tt.K = L.rank;
+            tt.trans_a = 0;
+            tt.src = 0;
+            tt.blk = (int)b;
+            tt.x_row0 = 0;
+            per[t0 / R].push_back(tt);
+        }
+    }
+    for (const LeafDesc &L : p->leaves) {
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += R) {
+            TileTerm tt;
+            tt.lda = L.b;
+            tt.K = L.b;
+            tt.src = 1;
+            tt.blk = -1;
+            tt.x_row0 = L.row0;
+            if (!trans) {
+                tt.a = L.d + (t0 - L.row0);
+                tt.trans_a = 0;
+            } else {
+                tt.a = L.d + (long long)(t0 - L.row0) * L.b;
+                tt.trans_a = 1;
+            }
+            per[t0 / R].push_back(tt);
+        }
+    }
+    S.tile_row0.resize(ntiles);
+    S.tile_begin.assign(ntiles + 1, 0);
+    S.terms.clear();
+    for (int t = 0; t < ntiles; ++t) {
+        S.tile_row0[t] = t * R;
+        S.tile_begin[t] = (int)S.terms.size();
+        S.terms.insert(S.terms.end(), per[t].begin(), per[t].end());
+    }
+    S.tile_begin[ntiles] = (int)S.terms.size();
+}
+
+template <class T>
+static int upload_vec(const std::vector<T> &v, T **dst, long long *bytes)
+{
+    size_t n = std::max<size_t>(v.size(), 1);
+    DG_CUDA(cudaMalloc((void **)dst, n * sizeof(T)));
+    *bytes += (long long)(n * sizeof(T));
+    if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+static int upload_schedule(Schedule &S, long long *bytes)
+{
+    int rc;
+    if ((rc = upload_vec(S.items, &S.d_items, bytes))) return rc;
+    if ((rc = upload_vec(S.poff, &S.d_poff, bytes))) return rc;
+    if ((rc = upload_vec(S.chunks_of, &S.d_chunks, bytes))) return rc;
+    if ((rc = upload_vec(S.tile_row0, &S.d_tile_row0, bytes))) return rc;
+    if ((rc = upload_vec(S.tile_begin, &S.d_tile_begin, bytes))) return rc;
+    return upload_vec(S.terms, &S.d_terms, bytes);
+}
+
+// Copy live factor values from the host tree into the pool, in the same
+// pre-order as Builder::walk.
+struct Uploader {
+    Plan *p;
+    cudaStream_t st;
+    size_t lr_i = 0, leaf_i = 0;
+    int walk(const DPlrMtx *A)
+    {
+        if (A->type == PLR_DMTX) {
+            const LeafDesc &L = p->leaves[leaf_i++];
+            if (L.b > 0)
+                DG_CUDA(cudaMemcpyAsync(p->pool + L.d, A->dd.d, sizeof(double) * L.b * L.b,
+                                        cudaMemcpyHostToDevice, st));
+            return 0;
+        }
+        for (int s = 0; s < 2; ++s) {
+            const DPlrMtx *B = s == 0 ? A->dh.ne : A->dh.sw;
+            const LRDesc &L = p->lr[lr_i++];
+            if (B->dlr.rank != L.rank || B->size != L.n)
+                return fail(DPLR_GPU_EINVAL, "plan refresh: structure or rank changed");
+            size_t cnt = (size_t)L.n * L.rank;
+            if (cnt) {
+                DG_CUDA(cudaMemcpyAsync(p->pool + L.u, B->dlr.u, cnt * sizeof(double),
+                                        cudaMemcpyHostToDevice, st));
+                DG_CUDA(cudaMemcpyAsync(p->pool + L.v, B->dlr.v, cnt * sizeof(double),
+                                        cudaMemcpyHostToDevice, st));
+                DG_CUDA(cudaMemcpyAsync(p->pool + L.sig, B->dlr.sig, L.rank * sizeof(double),
+                                        cudaMemcpyHostToDevice, st));
+            }
+        }
+        int rc = walk(A->dh.nw);
+        if (rc) return rc;
+        return walk(A->dh.se);
+    }
+};
+
+int plan_upload_values(Plan *p, const DPlrMtx *A, cudaStream_t st)
+{
+    if (!A || A->size != p->m) return fail(DPLR_GPU_EINVAL, "plan refresh: size mismatch");
+    int rc = validate_tree(p->m, A, "dplr_gpu_plan_refresh");
+    if (rc) return rc;
+    Uploader up{p, st};
+    rc = up.walk(A);
+    if (rc) return rc;
+    if (up.lr_i != p->lr.size() || up.leaf_i != p->leaves.size())
+        return fail(DPLR_GPU_EINVAL, "plan refresh: structure changed");
+    DG_CUDA(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out)
+{
+    int rc = validate_tree(m, A, "dplr_gpu_plan_create");
+    if (rc) return rc;
+    Plan *p = new Plan();
+    p->m = m;
+    Builder b{p};
+    b.walk(A, 0, 0);
+    build_schedule(p, 0, p->sched[0]);
+    build_schedule(p, 1, p->sched[1]);
+    long long bytes = 0;
+    size_t pool_bytes = (size_t)std::max<long long>(p->pool_doubles, 1) * sizeof(double);
+    cudaError_t e = cudaMalloc((void **)&p->pool, pool_bytes);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return fail(DPLR_GPU_ENOMEM, "plan: cannot allocate %zu bytes of factor pool: %s",
+                    pool_bytes, cudaGetErrorString(e));
+    }
+    bytes += (long long)pool_bytes;
+    if ((rc = upload_vec(p->lr, &p->d_lr, &bytes)) || (rc = upload_vec(p->leaves, &p->d_leaves, &bytes)) ||
+        (rc = upload_schedule(p->sched[0], &bytes)) || (rc = upload_schedule(p->sched[1], &bytes))) {
+        plan_free(p);
+        return rc;
+    }
+    p->device_bytes = bytes;
+    Uploader up{p, st};
+    rc = up.walk(A);
+    if (!rc) {
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e2 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "plan upload: %s", cudaGetErrorString(e2));
+    }
+    if (rc) {
+        plan_free(p);
+        return rc;
+    }
+    *out = p;
+    return 0;
+}
+
+static void free_schedule(Schedule &S)
+{
+    cudaFree(S.d_items);
+    cudaFree(S.d_poff);
+    cudaFree(S.d_chunks);
+    cudaFree(S.d_tile_row0);
+    cudaFree(S.d_tile_begin);
+    cudaFree(S.d_terms);
+}
+
+void factor_free(Plan *p);   // factor.cu
+
+void plan_free(Plan *p)
+{
+    if (!p) return;
+    factor_free(p);
+    cudaFree(p->pool);
+    cudaFree(p->d_lr);
+    cudaFree(p->d_leaves);
+    free_schedule(p->sched[0]);
+    free_schedule(p->sched[1]);
+    cudaFree(p->work);
+    cudaFree(p->xbuf);
+    cudaFree(p->ybuf);
+    delete p;
+}
+
+int ensure_buffer(double **buf, size_t *have, size_t need)
+{
+    if (need <= *have && *buf) return 0;
+    if (*buf) cudaFree(*buf);
+    *buf = nullptr;
+    *have = 0;
+    size_t n = std::max<size_t>(need, 1);
+    cudaError_t e = cudaMalloc((void **)buf, n * sizeof(double));
+    if (e != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "cannot allocate %zu bytes of device scratch: %s",
+                    n * sizeof(double), cudaGetErrorString(e));
+    *have = n;
+    return 0;
+}
+
+}  // namespace dg

@@ -1,0 +1,70 @@
+/*
+ * dplr_gb300.h -- GPU additions to the DPLR interface (libdplr_gb300.so).
+ *
+ * None of these exist in DPLR; the drop-in entry points of dplr.h are
+ * built on them.  All pointers are plain C pointers; `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream); device
+ * arrays are column-major FP64 with a leading dimension.
+ *
+ * A plan is a device-resident copy of one PLR matrix: a block table
+ * (one descriptor per low-rank block and per dense leaf) plus one
+ * contiguous factor pool in HBM.  Building a plan uploads the tree once;
+ * every later apply or solve through the plan reads only device memory.
+ * The drop-in dplrgepmv/dplrgepdmm upload the tree on every call unless
+ * it was registered with dplr_gpu_register(), in which case they reuse
+ * the registered plan (call dplr_gpu_register() again after modifying the
+ * tree on the host).
+ *
+ * Every function returns 0 on success and a negative DPLR_GPU_E* code on
+ * failure; dplr_gpu_last_error() describes the last failure of the
+ * calling thread.  A plan must not be used by two threads at once;
+ * distinct plans are independent.
+ */
+#ifndef DPLR_GB300_EXT_H
+#define DPLR_GB300_EXT_H
+
+#include "dplr.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPLR_GPU_OK          0
+#define DPLR_GPU_EINVAL     -1   /* bad argument (size, type, stride ...) */
+#define DPLR_GPU_ECUDA      -2   /* CUDA runtime error */
+#define DPLR_GPU_ENOMEM     -3   /* device or host allocation failed */
+#define DPLR_GPU_ESINGULAR  -4   /* zero pivot in a leaf or capacitance LU */
+#define DPLR_GPU_ENOTCONV   -5   /* refinement did not reach the tolerance */
+#define DPLR_GPU_ESTATE     -6   /* plan not factored / wrong state */
+
+typedef struct dplr_gpu_plan_s *dplr_gpu_plan;
+
+/* Thread-local description of the last failure ("" if none). */
+DPLR_API const char *dplr_gpu_last_error(void);
+
+/* Build a plan from an m x m host tree (upload of all factors). */
+DPLR_API int dplr_gpu_plan_create(int m, const DPlrMtx *A, void *stream, dplr_gpu_plan *plan);
+DPLR_API void dplr_gpu_plan_destroy(dplr_gpu_plan plan);
+/* Re-upload factor values from the host tree (same structure and ranks). */
+DPLR_API int dplr_gpu_plan_refresh(dplr_gpu_plan plan, const DPlrMtx *A, void *stream);
+/* Size and stored entries (dplrnz) of the planned matrix. */
+DPLR_API int dplr_gpu_plan_info(dplr_gpu_plan plan, int *m, long long *nnz, int *levels,
+                       int *max_rank);
+/* Device bytes held by the plan (factors, tables, factorisation, scratch). */
+DPLR_API long long dplr_gpu_plan_device_bytes(dplr_gpu_plan plan);
+
+/* Y := alpha*op(A)*X + beta*Y on device arrays (X: m x n, ldx >= m;
+ * Y: m x n, ldy >= m).  beta == 0 does not read Y. */
+DPLR_API int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha, const double *X,
+                   int ldx, double beta, double *Y, int ldy, void *stream);
+
+/* Associate the drop-in entry points with a plan for this host tree
+ * (they then skip the upload).  dplr_gpu_unregister drops the link. */
+DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);
+DPLR_API int dplr_gpu_unregister(DPlrMtx *A);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DPLR_GB300_EXT_H */
