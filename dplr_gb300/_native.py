@@ -39,6 +39,21 @@ def _bind(lib: ctypes.CDLL) -> None:
                                   c_void_p, c_int, c_void_p])
     sig("dplr_gpu_register", c_int, [c_int, PDPlrMtx])
     sig("dplr_gpu_unregister", c_int, [PDPlrMtx])
+    sig("dplr_gpu_factor", c_int, [c_void_p, c_int, c_void_p])
+    sig("dplr_gpu_factor_device_bytes", c_longlong, [c_void_p])
+    sig("dplr_gpu_solve", c_int, [c_void_p, c_char, c_int, c_void_p, c_int, c_void_p, c_int,
+                                  c_void_p])
+    sig("dplr_gpu_solve_refined", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
+                                          c_double, c_int, POINTER(c_double), POINTER(c_int),
+                                          c_void_p])
+    sig("dplr_gpu_solve_refined_host", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
+                                               c_double, c_int, POINTER(c_double), POINTER(c_int),
+                                               c_void_p])
+    sig("dplr_gpu_launch_count", c_longlong, [])
+    sig("dplr_gpu_profile_start", c_int, [])
+    sig("dplr_gpu_profile_stop", c_int, [])
+    sig("dplr_gpu_profile_entry", c_int, [c_int, POINTER(ctypes.c_char_p), POINTER(c_double),
+                                          POINTER(c_double), POINTER(c_double), POINTER(c_int)])
     for name, res, args in _OPTIONAL:
         if hasattr(lib, name):
             sig(name, res, args)
@@ -67,6 +82,28 @@ def api() -> PlrApi:
     if _api is None:
         _api = PlrApi(lib(), "dplr")
     return _api
+
+
+def launch_count() -> int:
+    return int(lib().dplr_gpu_launch_count())
+
+
+def profile_start() -> None:
+    check(lib().dplr_gpu_profile_start(), "dplr_gpu_profile_start")
+
+
+def profile_stop() -> dict:
+    """Per kernel kind: {name: (ms, flops, bytes, launches)} since profile_start()."""
+    n = lib().dplr_gpu_profile_stop()
+    if n < 0:
+        check(n, "dplr_gpu_profile_stop")
+    out = {}
+    for i in range(n):
+        name, ms, fl, by, la = ctypes.c_char_p(), c_double(), c_double(), c_double(), c_int()
+        check(lib().dplr_gpu_profile_entry(i, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(fl),
+                                           ctypes.byref(by), ctypes.byref(la)), "profile entry")
+        out[name.value.decode()] = (ms.value, fl.value, by.value, la.value)
+    return out
 
 
 def last_error() -> str:

@@ -12,10 +12,13 @@
 // rows of op(B) are rejected (DPLR reads out of bounds for them).
 #include "internal.cuh"
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <string>
+#include <vector>
 
 namespace dg {
 const char *last_error_c();
@@ -249,6 +252,109 @@ void dplrgepdmm(char transa, char transb, int m, int n, double *alpha, DPlrMtx *
         return report(fn);
     if (apply_device(p, ta, n, *alpha, p->xbuf, m, *beta, p->ybuf, m, 0, false)) return report(fn);
     if (download_matrix(C, 1, ldc, p->ybuf, m, n)) return report(fn);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------- instrumentation
+namespace dg {
+
+static std::atomic<long long> g_launches{0};
+static std::atomic<int> g_prof_on{0};
+struct ProfRec {
+    const char *name;
+    cudaEvent_t e0, e1;
+    double flops, bytes;
+};
+static std::mutex g_prof_mu;
+static std::vector<ProfRec> g_prof;
+struct ProfAgg {
+    std::string name;
+    double ms = 0, flops = 0, bytes = 0;
+    int launches = 0;
+};
+static std::vector<ProfAgg> g_prof_out;
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+ProfScope::ProfScope(const char *name, cudaStream_t st, double flops, double bytes)
+{
+    if (!g_prof_on.load()) return;
+    ProfRec r{name, nullptr, nullptr, flops, bytes};
+    if (cudaEventCreate(&r.e0) != cudaSuccess || cudaEventCreate(&r.e1) != cudaSuccess) return;
+    cudaEventRecord(r.e0, st);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    id = (int)g_prof.size();
+    g_prof.push_back(r);
+    stream_ = st;
+}
+
+ProfScope::~ProfScope()
+{
+    if (id < 0) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEventRecord(g_prof[id].e1, stream_);
+}
+
+}  // namespace dg
+
+extern "C" {
+
+long long dplr_gpu_launch_count(void) { return dg::g_launches.load(); }
+
+int dplr_gpu_profile_start(void)
+{
+    std::lock_guard<std::mutex> lk(dg::g_prof_mu);
+    for (auto &r : dg::g_prof) {
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    dg::g_prof.clear();
+    dg::g_prof_out.clear();
+    dg::g_prof_on.store(1);
+    return 0;
+}
+
+int dplr_gpu_profile_stop(void)
+{
+    dg::g_prof_on.store(0);
+    std::lock_guard<std::mutex> lk(dg::g_prof_mu);
+    dg::g_prof_out.clear();
+    for (auto &r : dg::g_prof) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(r.e1) != cudaSuccess || cudaEventElapsedTime(&ms, r.e0, r.e1) != cudaSuccess)
+            return fail(DPLR_GPU_ECUDA, "profile: event timing failed");
+        dg::ProfAgg *a = nullptr;
+        for (auto &x : dg::g_prof_out)
+            if (x.name == r.name) a = &x;
+        if (!a) {
+            dg::g_prof_out.push_back(dg::ProfAgg());
+            a = &dg::g_prof_out.back();
+            a->name = r.name;
+        }
+        a->ms += ms;
+        a->flops += r.flops;
+        a->bytes += r.bytes;
+        a->launches += 1;
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    dg::g_prof.clear();
+    return (int)dg::g_prof_out.size();
+}
+
+int dplr_gpu_profile_entry(int i, const char **name, double *ms, double *flops, double *bytes,
+                           int *launches)
+{
+    std::lock_guard<std::mutex> lk(dg::g_prof_mu);
+    if (i < 0 || i >= (int)dg::g_prof_out.size()) return fail(DPLR_GPU_EINVAL, "profile: no entry %d", i);
+    const dg::ProfAgg &a = dg::g_prof_out[i];
+    if (name) *name = a.name.c_str();
+    if (ms) *ms = a.ms;
+    if (flops) *flops = a.flops;
+    if (bytes) *bytes = a.bytes;
+    if (launches) *launches = a.launches;
+    return 0;
 }
 
 }  // extern "C"

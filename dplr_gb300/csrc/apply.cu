@@ -30,9 +30,8 @@ constexpr int kRankTile = 64; // ranks handled per pass of the panel kernel
 // four row groups are summed through shared memory at the end.
 template <int NB>
 __global__ void __launch_bounds__(kThreads) panel_kernel(
-    const LRDesc *__restrict__ lr, const PanelItem *__restrict__ items,
-    const long long *__restrict__ poff, const double *__restrict__ pool,
-    const double *__restrict__ X, int ldx, int nrhs, int trans, double *__restrict__ partials)
+    const PanelItem *__restrict__ items, const double *__restrict__ fbase,
+    const double *__restrict__ X, int ldx, int nrhs, double *__restrict__ partials)
 {
     constexpr int kStage = kSlab * (kRankTile + 1) + kSlab * NB;
     constexpr int kRed = 4 * kRankTile * NB;
@@ -42,17 +41,15 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
     double(*red)[kRankTile][NB] = reinterpret_cast<double(*)[kRankTile][NB]>(sm);
 
     const PanelItem it = items[blockIdx.x];
-    const LRDesc L = lr[it.blk];
-    const double *F = pool + (trans ? L.u : L.v);
-    const int in0 = trans ? L.row0 : L.col0;
+    const double *F = fbase + it.f;
     const int j0 = blockIdx.y * NB;
     const int nj = min(NB, nrhs - j0);
     const int t = threadIdx.x;
     const int kk = t % kRankTile, g = t / kRankTile;
-    double *P = partials + poff[it.blk] * nrhs + (long long)it.chunk * L.rank * nrhs;
+    double *P = partials + it.p * nrhs + (long long)it.chunk * it.rank * nrhs;
 
-    for (int kt = 0; kt < L.rank; kt += kRankTile) {
-        const int nk = min(kRankTile, L.rank - kt);
+    for (int kt = 0; kt < it.rank; kt += kRankTile) {
+        const int nk = min(kRankTile, it.rank - kt);
         double acc[NB];
 #pragma unroll
         for (int j = 0; j < NB; ++j) acc[j] = 0.0;
@@ -61,12 +58,12 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
             __syncthreads();
             for (int e = t; e < kSlab * kRankTile; e += kThreads) {
                 int r = e % kSlab, c = e / kSlab;
-                Fs[r][c] = (r < ns && c < nk) ? F[(long long)(kt + c) * L.n + it.r0 + s0 + r] : 0.0;
+                Fs[r][c] = (r < ns && c < nk) ? F[(long long)(kt + c) * it.n + it.r0 + s0 + r] : 0.0;
             }
             for (int e = t; e < kSlab * NB; e += kThreads) {
                 int r = e % kSlab, c = e / kSlab;
                 Xs[r][c] = (r < ns && c < nj)
-                               ? X[(long long)(j0 + c) * ldx + in0 + it.r0 + s0 + r]
+                               ? X[(long long)(j0 + c) * ldx + it.in0 + it.r0 + s0 + r]
                                : 0.0;
             }
             __syncthreads();
@@ -84,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
         if (g == 0 && kk < nk) {
             for (int j = 0; j < nj; ++j) {
                 double s = red[0][kk][j] + red[1][kk][j] + red[2][kk][j] + red[3][kk][j];
-                P[(kt + kk) + (long long)(j0 + j) * L.rank] = s;
+                P[(kt + kk) + (long long)(j0 + j) * it.rank] = s;
             }
         }
         __syncthreads();
@@ -92,23 +89,21 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
 }
 
 // ---------------------------------------------------------------- reduce
-// T_b[k, j] = sig[k] * sum_c P_b[c][k, j]; grid.x = block index.
-__global__ void reduce_kernel(const LRDesc *__restrict__ lr, const long long *__restrict__ poff,
-                              const int *__restrict__ chunks, const double *__restrict__ pool,
+// T[k, j] = sig[k] * sum_c P[c][k, j]; grid.x = reduce item.
+__global__ void reduce_kernel(const ReduceItem *__restrict__ items,
+                              const double *__restrict__ sigbase,
                               const double *__restrict__ partials, int nrhs,
                               double *__restrict__ T)
 {
-    const int b = blockIdx.x;
-    const LRDesc L = lr[b];
-    const long long cnt = (long long)L.rank * nrhs;
+    const ReduceItem R = items[blockIdx.x];
+    const long long cnt = (long long)R.rank * nrhs;
     const long long e = (long long)blockIdx.y * blockDim.x + threadIdx.x;
     if (e >= cnt) return;
-    const int k = (int)(e % L.rank);
-    const double *P = partials + poff[b] * nrhs + e;
+    const int k = (int)(e % R.rank);
+    const double *P = partials + R.p * nrhs + e;
     double s = 0.0;
-    const int nch = chunks[b];
-    for (int c = 0; c < nch; ++c) s += P[(long long)c * cnt];
-    T[(long long)L.toff * nrhs + e] = pool[L.sig + k] * s;
+    for (int c = 0; c < R.nch; ++c) s += P[(long long)c * cnt];
+    T[R.t * nrhs + e] = R.sig >= 0 ? sigbase[R.sig + k] * s : s;
 }
 
 // ---------------------------------------------------------------- expand
@@ -117,10 +112,10 @@ __global__ void reduce_kernel(const LRDesc *__restrict__ lr, const long long *__
 // groups are combined through shared memory before the write-back.
 template <int NB>
 __global__ void __launch_bounds__(kThreads) expand_kernel(
-    const double *__restrict__ pool, const TileTerm *__restrict__ terms,
+    const double *__restrict__ abase, const TileTerm *__restrict__ terms,
     const int *__restrict__ tile_row0, const int *__restrict__ tile_begin,
-    const LRDesc *__restrict__ lr, const double *__restrict__ T, const double *__restrict__ X,
-    int ldx, double *__restrict__ Y, int ldy, int nrhs, int R, double alpha, double beta)
+    const double *__restrict__ T, const double *__restrict__ X, int ldx, double *__restrict__ Y,
+    int ldy, int nrhs, int R, double alpha, double beta)
 {
     constexpr int kStage = 64 * (kSlab + 1) + kSlab * NB;
     constexpr int kRed = kThreads * NB;
@@ -143,13 +138,15 @@ __global__ void __launch_bounds__(kThreads) expand_kernel(
 
     for (int q = tile_begin[tile]; q < tile_begin[tile + 1]; ++q) {
         const TileTerm tt = terms[q];
-        const double *A = pool + tt.a;
+        const double *A = abase + tt.a;
         const double *B;
         long long ldb;
         if (tt.src == 0) {
-            const LRDesc L = lr[tt.blk];
-            B = T + (long long)L.toff * nrhs + (long long)j0 * L.rank;
-            ldb = L.rank;
+            B = T + tt.b * nrhs + (long long)j0 * tt.ldb;
+            ldb = tt.ldb;
+        } else if (tt.src == 2) {
+            B = T + tt.b + (long long)j0 * tt.ldb;
+            ldb = tt.ldb;
         } else {
             B = X + tt.x_row0 + (long long)j0 * ldx;
             ldb = ldx;
@@ -195,6 +192,68 @@ __global__ void __launch_bounds__(kThreads) expand_kernel(
     }
 }
 
+// ----------------------------------------------------------- capacitance
+// W[i, j] = s_i * sum_k op(Kinv)[i, k] * [T1; T2][k, j] for one H node
+// (s_i = 1 unless scaled); grid (node, rhs tile), thread per (i, j-group).
+template <int NB>
+__global__ void __launch_bounds__(kThreads) cap_kernel(
+    const CapItem *__restrict__ items, const double *__restrict__ kbase,
+    const double *__restrict__ sigbase, int trans, int scaled, const double *__restrict__ T,
+    double *__restrict__ W, int nrhs)
+{
+    constexpr int KC = 256;            // rows of [T1; T2] staged per pass
+    __shared__ double Ts[KC][NB];
+    const CapItem c = items[blockIdx.x];
+    const int r = c.r1 + c.r2;
+    const int j0 = blockIdx.y * NB;
+    const int nj = min(NB, nrhs - j0);
+    const double *K = kbase + c.k;
+    // Each thread owns output rows i = tid, tid + 256, ... (at most 4).
+    double acc[4][NB];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) acc[q][j] = 0.0;
+    for (int k0 = 0; k0 < r; k0 += KC) {
+        const int nk = min(KC, r - k0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < KC * NB; e += blockDim.x) {
+            int k = e % KC, j = e / KC;
+            double v = 0.0;
+            if (j < nj && k < nk) {
+                int kk = k0 + k;
+                v = kk < c.r1 ? T[c.t1 * nrhs + kk + (long long)(j0 + j) * c.r1]
+                              : T[c.t2 * nrhs + (kk - c.r1) + (long long)(j0 + j) * c.r2];
+            }
+            Ts[k][j] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = threadIdx.x + q * blockDim.x;
+            if (i >= r) break;
+            for (int k = 0; k < nk; ++k) {
+                const int kk = k0 + k;
+                double a = trans ? K[kk + (long long)i * r] : K[i + (long long)kk * r];
+#pragma unroll
+                for (int j = 0; j < NB; ++j) acc[q][j] = fma(a, Ts[k][j], acc[q][j]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = threadIdx.x + q * blockDim.x;
+        if (i >= r) break;
+        double s = 1.0;
+        if (scaled) s = i < c.r1 ? sigbase[c.s1 + i] : sigbase[c.s2 + i - c.r1];
+        for (int j = 0; j < nj; ++j) {
+            double *w = i < c.r1 ? W + c.t1 * nrhs + i + (long long)(j0 + j) * c.r1
+                                 : W + c.t2 * nrhs + (i - c.r1) + (long long)(j0 + j) * c.r2;
+            *w = s * acc[q][j];
+        }
+    }
+}
+
 // ------------------------------------------------------------- utilities
 __global__ void scale_kernel(double *Y, int rows, int cols, int ldy, double beta)
 {
@@ -229,6 +288,7 @@ int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream
     long long n = (long long)rows * cols;
     int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
     scale_kernel<<<grid, 256, 0, st>>>(Y, rows, cols, ldy, beta);
+    note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
 }
@@ -240,36 +300,109 @@ int transpose_device(const double *src, int rows, int cols, int lds, double *dst
     if (rows <= 0 || cols <= 0) return 0;
     dim3 grid((rows + 31) / 32, (cols + 31) / 32), block(32, 8);
     transpose_kernel<<<grid, block, 0, st>>>(src, rows, cols, lds, dst, ldd);
+    note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
 }
 
-template <int NB>
-static int launch_apply(Plan *p, const Schedule &S, int trans, int nrhs, double alpha,
-                        const double *X, int ldx, double beta, double *Y, int ldy,
-                        cudaStream_t st)
+static int pick_nb(int nrhs)
 {
-    double *T = p->work;
-    double *partials = p->work + (size_t)p->total_rank * nrhs;
-    const int ntile_rhs = (nrhs + NB - 1) / NB;
-    if (!S.items.empty()) {
-        dim3 g1((unsigned)S.items.size(), ntile_rhs);
-        panel_kernel<NB><<<g1, kThreads, 0, st>>>(p->d_lr, S.d_items, S.d_poff, p->pool, X, ldx,
-                                                   nrhs, trans, partials);
-        DG_CUDA(cudaGetLastError());
-        long long maxcnt = (long long)p->max_rank * nrhs;
-        dim3 g2((unsigned)p->lr.size(), (unsigned)((maxcnt + 255) / 256));
-        reduce_kernel<<<g2, 256, 0, st>>>(p->d_lr, S.d_poff, S.d_chunks, p->pool, partials, nrhs, T);
-        DG_CUDA(cudaGetLastError());
+    return nrhs >= 16 ? 16 : nrhs >= 8 ? 8 : nrhs >= 4 ? 4 : nrhs >= 2 ? 2 : 1;
+}
+
+#define DG_DISPATCH_NB(nb, CALL)                                                   \
+    switch (nb) {                                                                  \
+    case 16: { constexpr int NB = 16; CALL; } break;                               \
+    case 8: { constexpr int NB = 8; CALL; } break;                                 \
+    case 4: { constexpr int NB = 4; CALL; } break;                                 \
+    case 2: { constexpr int NB = 2; CALL; } break;                                 \
+    default: { constexpr int NB = 1; CALL; } break;                                \
     }
+
+int run_panel(const Schedule &S, const double *fbase, const double *X, int ldx, int nrhs,
+              double *partials, cudaStream_t st)
+{
+    if (S.items.empty() || nrhs <= 0) return 0;
+    const int nb = pick_nb(nrhs);
+    dim3 g((unsigned)S.items.size(), (unsigned)((nrhs + nb - 1) / nb));
+    double fl = 0, by = 0;
+    for (const PanelItem &it : S.items) {
+        fl += 2.0 * it.len * it.rank * nrhs;
+        by += 8.0 * ((double)it.len * it.rank + (double)it.len * nrhs + (double)it.rank * nrhs);
+    }
+    ProfScope ps("panel", st, fl, by);
+    DG_DISPATCH_NB(nb, (panel_kernel<NB><<<g, kThreads, 0, st>>>(S.d_items, fbase, X, ldx, nrhs,
+                                                                  partials)));
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int run_reduce(const Schedule &S, const double *sigbase, const double *partials, int nrhs,
+               double *T, cudaStream_t st)
+{
+    if (S.reduces.empty() || nrhs <= 0 || S.max_rank <= 0) return 0;
+    long long maxcnt = (long long)S.max_rank * nrhs;
+    dim3 g((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256));
+    double fl = 0, by = 0;
+    for (const ReduceItem &r : S.reduces) {
+        fl += (double)r.nch * r.rank * nrhs;
+        by += 8.0 * (r.nch + 1.0) * r.rank * nrhs;
+    }
+    ProfScope ps("reduce", st, fl, by);
+    reduce_kernel<<<g, 256, 0, st>>>(S.d_reduces, sigbase, partials, nrhs, T);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int run_expand(const Schedule &S, const double *abase, const double *T, const double *X, int ldx,
+               double *Y, int ldy, int nrhs, double alpha, double beta, cudaStream_t st)
+{
     const int ntiles = (int)S.tile_row0.size();
-    if (ntiles > 0) {
-        dim3 g3(ntiles, ntile_rhs);
-        expand_kernel<NB><<<g3, kThreads, 0, st>>>(p->pool, S.d_terms, S.d_tile_row0,
-                                                   S.d_tile_begin, p->d_lr, T, X, ldx, Y, ldy,
-                                                   nrhs, S.tile_rows, alpha, beta);
-        DG_CUDA(cudaGetLastError());
+    if (ntiles == 0 || nrhs <= 0) return 0;
+    const int nb = pick_nb(nrhs);
+    dim3 g(ntiles, (unsigned)((nrhs + nb - 1) / nb));
+    double fl = 0, by = 8.0 * ntiles * S.tile_rows * nrhs * (beta == 0.0 ? 1.0 : 2.0);
+    for (const TileTerm &t : S.terms) {
+        fl += 2.0 * S.tile_rows * t.K * nrhs;
+        by += 8.0 * ((double)S.tile_rows * t.K + (double)t.K * nrhs);
     }
+    ProfScope ps("expand", st, fl, by);
+    note_launch();
+    DG_DISPATCH_NB(nb, (expand_kernel<NB><<<g, kThreads, 0, st>>>(
+                           abase, S.d_terms, S.d_tile_row0, S.d_tile_begin, T, X, ldx, Y, ldy,
+                           nrhs, S.tile_rows, alpha, beta)));
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int trans,
+             const double *T, double *W, int nrhs, cudaStream_t st)
+{
+    if (S.caps.empty() || nrhs <= 0) return 0;
+    for (const CapItem &c : S.caps)
+        if (c.r1 + c.r2 > 4 * kThreads)
+            return fail(DPLR_GPU_EINVAL, "capacitance of order %d exceeds %d", c.r1 + c.r2,
+                        4 * kThreads);
+    const int nb = std::min(pick_nb(nrhs), 8);
+    dim3 g((unsigned)S.caps.size(), (unsigned)((nrhs + nb - 1) / nb));
+    const int scaled = sigbase != nullptr;
+    double fl = 0, by = 0;
+    for (const CapItem &c : S.caps) {
+        double r = c.r1 + c.r2;
+        fl += 2.0 * r * r * nrhs;
+        by += 8.0 * (r * r + 2.0 * r * nrhs);
+    }
+    ProfScope ps("capacitance", st, fl, by);
+    note_launch();
+    switch (nb) {
+    case 8: cap_kernel<8><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    case 4: cap_kernel<4><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    case 2: cap_kernel<2><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    default: cap_kernel<1><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    }
+    DG_CUDA(cudaGetLastError());
     return 0;
 }
 
@@ -285,14 +418,14 @@ int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, in
         return rc;
     }
     const Schedule &S = p->sched[trans ? 1 : 0];
-    size_t need = (size_t)(p->total_rank + S.partial_per_rhs) * nrhs;
+    size_t need = (size_t)(S.t_per_rhs + S.partial_per_rhs) * nrhs;
     int rc = ensure_buffer(&p->work, &p->work_doubles, need);
     if (rc) return rc;
-    if (nrhs >= 16) return launch_apply<16>(p, S, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
-    if (nrhs >= 8) return launch_apply<8>(p, S, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
-    if (nrhs >= 4) return launch_apply<4>(p, S, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
-    if (nrhs >= 2) return launch_apply<2>(p, S, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
-    return launch_apply<1>(p, S, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
+    double *T = p->work;
+    double *partials = p->work + (size_t)S.t_per_rhs * nrhs;
+    if ((rc = run_panel(S, p->pool, X, ldx, nrhs, partials, st))) return rc;
+    if ((rc = run_reduce(S, p->pool, partials, nrhs, T, st))) return rc;
+    return run_expand(S, p->pool, T, X, ldx, Y, ldy, nrhs, alpha, beta, st);
 }
 
 }  // namespace dg

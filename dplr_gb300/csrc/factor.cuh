@@ -1,0 +1,54 @@
+// factor.cuh -- Woodbury factorisation state shared by factor.cu,
+// solve.cu and inverse.cu.
+#pragma once
+
+#include "internal.cuh"
+
+namespace dg {
+
+struct LevelOps {
+    Schedule n;       // op N: panels on V, caps K^-1, updates with Z_l
+    Schedule t;       // op T: panels on U, caps K^-T scaled, updates with Zt_l
+    int width = 0;    // r_l
+    std::vector<int> blocks;   // LRDesc indices at this level
+    std::vector<int> nodes;    // HDesc indices at this level
+};
+
+struct Fact {
+    int flags = 0;
+    bool transposed = false;
+    std::vector<LevelOps> lv;
+    std::vector<long long> zoff;      // per level, offset in zpool / ztpool
+    long long zdoubles = 0;
+    double *zpool = nullptr, *ztpool = nullptr;
+    std::vector<long long> koff;      // per node
+    long long kdoubles = 0;
+    double *kpool = nullptr;
+    std::vector<long long> leafoff;
+    long long leafdoubles = 0;
+    double *leafinv = nullptr;
+    Schedule leafN, leafT;            // expand schedules of the leaf step
+    // batched inverse tables
+    long long *d_koff = nullptr, *d_leafoff = nullptr;
+    int *d_ksize = nullptr, *d_leafsize = nullptr, *d_info = nullptr;
+    // scratch
+    double *work = nullptr;
+    size_t work_doubles = 0;
+    double *rhs = nullptr;            // factorisation right-hand sides (m x r_max)
+    size_t rhs_doubles = 0;
+    double *vec = nullptr;            // refinement vectors
+    size_t vec_doubles = 0;
+    long long bytes = 0;
+    // first singular matrix met while factoring: 0 none, 1 leaf, 2 capacitance
+    int sing_kind = 0, sing_index = -1, sing_info = 0;
+};
+
+
+int factor_build(Plan *p, int flags, cudaStream_t st);
+int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
+                 cudaStream_t st);
+long long factor_bytes(const Plan *p);
+int axpby_device(int m, int n, double a, const double *X, int ldx, double b, double *Y, int ldy,
+                 cudaStream_t st);
+
+}  // namespace dg

@@ -32,6 +32,19 @@ int fail(int code, const char *fmt, ...);
                               cudaGetErrorString(e_), __FILE__, __LINE__);         \
     } while (0)
 
+// ------------------------------------------------------- instrumentation
+// Every kernel launch of the library is counted; when profiling is on, the
+// main launch sites also bracket their launch with CUDA events on the
+// launching stream and record the algorithmic flops and bytes of that
+// launch (see prof_begin / prof_end in abi.cu).
+void note_launch();
+struct ProfScope {
+    int id = -1;
+    cudaStream_t stream_ = nullptr;
+    ProfScope(const char *name, cudaStream_t st, double flops, double bytes);
+    ~ProfScope();
+};
+
 // ---------------------------------------------------------------- tables
 struct LRDesc {            // one low-rank block U diag(sig) V^T
     long long u, v, sig;   // pool offsets (doubles)
@@ -55,35 +68,60 @@ struct HDesc {
     int parent;
 };
 
-// Work item of the panel kernel: rows [r0, r0+len) of block `blk`.
+// Work items below are self-contained (offsets, sizes, strides), so the same
+// kernels serve the apply (factors U/V of the pool) and the Woodbury solve
+// (factors V and the D^-1 W panels of the factorisation).
+
+// Panel item: partial F[r0:r0+len, 0:rank]^T X[in0+r0 : in0+r0+len, :]
+// written to partials + p*nrhs + chunk*rank*nrhs (rank x nrhs, ld rank).
 struct PanelItem {
-    int blk, r0, len, chunk;     // chunk index within the block
+    long long f;           // factor offset (column-major, ld n)
+    long long p;           // partial block offset / nrhs
+    int in0, n, rank, r0, len, chunk;
 };
 
-// One term of an output tile: acc += op(A)[tile rows, 0:K] * Bsrc[0:K, :]
+// Reduce item: T[t*nrhs + k + j*rank] = sig[k] * sum_c partial[c][k, j]
+// (no scaling when sig < 0).
+struct ReduceItem {
+    long long p, t, sig;
+    int rank, nch;
+};
+
+// Term of an output tile: acc += op(A)[tile rows, 0:K] * B[0:K, :]
 struct TileTerm {
-    long long a;       // pool offset of A's element (tile row 0, k = 0)
-    int lda;           // leading dimension of A
-    int K;             // inner size
-    int trans_a;       // 1: A element (i,k) at a + i*lda + k ; 0: a + i + k*lda
-    int src;           // 0: B = T buffer of block `blk`; 1: B = X rows from x_row0
-    int blk, x_row0;
+    long long a;           // offset of A's (tile row 0, k = 0) element
+    long long b;           // src 0: T buffer offset / nrhs (ld = ldb)
+    int lda, K;
+    int trans_a;           // 1: A(i,k) at a + i*lda + k ; 0: a + i + k*lda
+    int src;               // 0: B = T + b*nrhs; 1: B = X rows from x_row0; 2: B = T + b
+    int ldb, x_row0;
+};
+
+// Capacitance item of one H node: W = op(Kinv) [T1; T2] (optionally scaled
+// row-wise by [sig1; sig2]); W1, W2 are written at the offsets of T1, T2 in
+// the output buffer.
+struct CapItem {
+    long long k;           // offset of the r x r inverse (r = r1 + r2)
+    long long t1, t2;      // T / W offsets / nrhs (ld r1, r2)
+    long long s1, s2;      // sig offsets (pool) for the scaled variant
+    int r1, r2;
 };
 
 struct Schedule {
-    std::vector<PanelItem> items;     // host copy
-    std::vector<int> chunks_of;       // per block: number of panel chunks
-    std::vector<long long> poff;      // per block: prefix of chunks*rank (partials / nrhs)
-    long long partial_per_rhs = 0;    // total partial doubles / nrhs
+    std::vector<PanelItem> items;
+    std::vector<ReduceItem> reduces;
+    long long partial_per_rhs = 0;    // partial doubles / nrhs
+    long long t_per_rhs = 0;          // T buffer doubles / nrhs
     std::vector<int> tile_row0, tile_begin;   // tile_begin has ntiles+1 entries
     std::vector<TileTerm> terms;
+    std::vector<CapItem> caps;
     int tile_rows = 0;
-    // device copies
+    int max_rank = 0;
     PanelItem *d_items = nullptr;
-    long long *d_poff = nullptr;
-    int *d_chunks = nullptr;
+    ReduceItem *d_reduces = nullptr;
     int *d_tile_row0 = nullptr, *d_tile_begin = nullptr;
     TileTerm *d_terms = nullptr;
+    CapItem *d_caps = nullptr;
 };
 
 struct Plan {
@@ -115,7 +153,20 @@ void plan_free(Plan *p);
 int ensure_buffer(double **buf, size_t *have, size_t need);
 int validate_tree(int m, const DPlrMtx *A, const char *fn);
 
-// apply.cu
+// schedule helpers (plan.cu)
+int tile_rows_for(const Plan *p);
+int upload_schedule(Schedule &S, long long *bytes);
+void free_schedule(Schedule &S);
+
+// apply.cu: generic launches over a schedule
+int run_panel(const Schedule &S, const double *fbase, const double *X, int ldx, int nrhs,
+              double *partials, cudaStream_t st);
+int run_reduce(const Schedule &S, const double *sigbase, const double *partials, int nrhs,
+               double *T, cudaStream_t st);
+int run_expand(const Schedule &S, const double *abase, const double *T, const double *X, int ldx,
+               double *Y, int ldy, int nrhs, double alpha, double beta, cudaStream_t st);
+int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int trans,
+             const double *T, double *W, int nrhs, cudaStream_t st);
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,
                  double beta, double *Y, int ldy, cudaStream_t st, bool alpha0_squares_beta);
 int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream_t st);

@@ -144,41 +144,59 @@ struct Builder {
 
 static int gcd_int(int a, int b) { return b == 0 ? a : gcd_int(b, a % b); }
 
+// Tile height: a power of two (<= 64) dividing every leaf size, so every
+// block and leaf boundary falls on a tile boundary.
+int tile_rows_for(const Plan *p)
+{
+    int g = 0;
+    for (const LeafDesc &L : p->leaves) g = gcd_int(g, L.b);
+    int R = 64;
+    while (R > 1 && g > 0 && (g % R) != 0) R >>= 1;
+    return R;
+}
+
+// Apply schedule for op N (trans = 0) or op T (trans = 1): panels contract
+// V (U) with x over the block's input rows, tiles expand U (V) T_b over the
+// block's output rows plus the leaf term.
 static void build_schedule(Plan *p, int trans, Schedule &S)
 {
     const int CH = p->chunk_rows;
     S.items.clear();
-    S.chunks_of.assign(p->lr.size(), 0);
-    S.poff.assign(p->lr.size(), 0);
+    S.reduces.clear();
     long long poff = 0;
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
-        S.poff[b] = poff;
         if (L.rank == 0 || L.n == 0) continue;
         int nch = (L.n + CH - 1) / CH;
-        S.chunks_of[b] = nch;
         for (int c = 0; c < nch; ++c) {
             PanelItem it;
-            it.blk = (int)b;
+            it.f = trans ? L.u : L.v;
+            it.p = poff;
+            it.in0 = trans ? L.row0 : L.col0;
+            it.n = L.n;
+            it.rank = L.rank;
             it.r0 = c * CH;
             it.len = std::min(CH, L.n - c * CH);
             it.chunk = c;
             S.items.push_back(it);
         }
+        ReduceItem r;
+        r.p = poff;
+        r.t = L.toff;
+        r.sig = L.sig;
+        r.rank = L.rank;
+        r.nch = nch;
+        S.reduces.push_back(r);
         poff += (long long)nch * L.rank;
     }
     S.partial_per_rhs = poff;
+    S.t_per_rhs = p->total_rank;
+    S.max_rank = p->max_rank;
 
-    // Tile height: a power of two (<= 64) dividing every leaf size, so every
-    // block and leaf boundary falls on a tile boundary.
-    int g = 0;
-    for (const LeafDesc &L : p->leaves) g = gcd_int(g, L.b);
-    int R = 64;
-    while (R > 1 && (g % R) != 0) R >>= 1;
+    const int R = tile_rows_for(p);
     S.tile_rows = R;
     int ntiles = p->m / R;
     std::vector<std::vector<TileTerm>> per(ntiles);
-    // Low-rank terms: the block's output rows are U's rows (op N) or V's (op T).
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
@@ -187,11 +205,12 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
         for (int t0 = out0; t0 < out0 + L.n; t0 += R) {
             TileTerm tt;
             tt.a = base + (t0 - out0);
+            tt.b = L.toff;
             tt.lda = L.n;
             tt.K = L.rank;
             tt.trans_a = 0;
             tt.src = 0;
-            tt.blk = (int)b;
+            tt.ldb = L.rank;
             tt.x_row0 = 0;
             per[t0 / R].push_back(tt);
         }
@@ -199,10 +218,11 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
     for (const LeafDesc &L : p->leaves) {
         for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += R) {
             TileTerm tt;
+            tt.b = 0;
             tt.lda = L.b;
             tt.K = L.b;
             tt.src = 1;
-            tt.blk = -1;
+            tt.ldb = 0;
             tt.x_row0 = L.row0;
             if (!trans) {
                 tt.a = L.d + (t0 - L.row0);
@@ -214,15 +234,15 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
             per[t0 / R].push_back(tt);
         }
     }
-    S.tile_row0.resize(ntiles);
-    S.tile_begin.assign(ntiles + 1, 0);
+    S.tile_row0.clear();
+    S.tile_begin.clear();
     S.terms.clear();
     for (int t = 0; t < ntiles; ++t) {
-        S.tile_row0[t] = t * R;
-        S.tile_begin[t] = (int)S.terms.size();
+        S.tile_row0.push_back(t * R);
+        S.tile_begin.push_back((int)S.terms.size());
         S.terms.insert(S.terms.end(), per[t].begin(), per[t].end());
     }
-    S.tile_begin[ntiles] = (int)S.terms.size();
+    S.tile_begin.push_back((int)S.terms.size());
 }
 
 template <class T>
@@ -235,15 +255,15 @@ static int upload_vec(const std::vector<T> &v, T **dst, long long *bytes)
     return 0;
 }
 
-static int upload_schedule(Schedule &S, long long *bytes)
+int upload_schedule(Schedule &S, long long *bytes)
 {
     int rc;
     if ((rc = upload_vec(S.items, &S.d_items, bytes))) return rc;
-    if ((rc = upload_vec(S.poff, &S.d_poff, bytes))) return rc;
-    if ((rc = upload_vec(S.chunks_of, &S.d_chunks, bytes))) return rc;
+    if ((rc = upload_vec(S.reduces, &S.d_reduces, bytes))) return rc;
     if ((rc = upload_vec(S.tile_row0, &S.d_tile_row0, bytes))) return rc;
     if ((rc = upload_vec(S.tile_begin, &S.d_tile_begin, bytes))) return rc;
-    return upload_vec(S.terms, &S.d_terms, bytes);
+    if ((rc = upload_vec(S.terms, &S.d_terms, bytes))) return rc;
+    return upload_vec(S.caps, &S.d_caps, bytes);
 }
 
 // Copy live factor values from the host tree into the pool, in the same
@@ -335,14 +355,19 @@ int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out)
     return 0;
 }
 
-static void free_schedule(Schedule &S)
+void free_schedule(Schedule &S)
 {
     cudaFree(S.d_items);
-    cudaFree(S.d_poff);
-    cudaFree(S.d_chunks);
+    cudaFree(S.d_reduces);
     cudaFree(S.d_tile_row0);
     cudaFree(S.d_tile_begin);
     cudaFree(S.d_terms);
+    cudaFree(S.d_caps);
+    S.d_items = nullptr;
+    S.d_reduces = nullptr;
+    S.d_tile_row0 = S.d_tile_begin = nullptr;
+    S.d_terms = nullptr;
+    S.d_caps = nullptr;
 }
 
 void factor_free(Plan *p);   // factor.cu

@@ -1,0 +1,179 @@
+// solve.cu -- factor / solve / refined-solve entry points.
+//
+// DPLR solves by forming B = inv(A) explicitly (dplrgeinv,
+// src/dplrinv.c:93) and applying it with dplrgepdmm.  The GPU library keeps
+// the Woodbury factorisation instead (factor.cu) and offers
+//   dplr_gpu_factor        build Z = D^-1 W, capacitance inverses, leaf inverses
+//   dplr_gpu_solve         X = op(A)^-1 B, one bottom-up sweep
+//   dplr_gpu_solve_refined X with ||B - A X|| / ||B|| <= tol per column,
+//                          by iterative refinement whose residual is the
+//                          FP64 PLR apply of the original matrix.
+#include "internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace dg {
+
+int factor_build(Plan *p, int flags, cudaStream_t st);
+int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
+                 cudaStream_t st);
+long long factor_bytes(const Plan *p);
+
+// Column 2-norms of an m x n matrix (one CTA per column).
+__global__ void colnorm_kernel(const double *A, int m, int lda, double *out)
+{
+    __shared__ double red[256];
+    const double *a = A + (long long)blockIdx.x * lda;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) s = fma(a[i], a[i], s);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(red[0]);
+}
+
+// Y (m x n) := X + alpha*Y  or plain copies, column-major with leading dims.
+__global__ void axpby_kernel(int m, int n, double a, const double *X, int ldx, double b, double *Y,
+                             int ldy)
+{
+    long long cnt = (long long)m * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % m), j = (int)(e / m);
+        double *y = Y + i + (long long)j * ldy;
+        double x = X[i + (long long)j * ldx];
+        *y = b == 0.0 ? a * x : fma(a, x, b * *y);
+    }
+}
+
+int axpby_device(int m, int n, double a, const double *X, int ldx, double b, double *Y, int ldy,
+                 cudaStream_t st)
+{
+    long long cnt = (long long)m * n;
+    if (cnt <= 0) return 0;
+    int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 16);
+    axpby_kernel<<<grid, 256, 0, st>>>(m, n, a, X, ldx, b, Y, ldy);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int colnorms_device(const double *A, int m, int n, int lda, double *out, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    colnorm_kernel<<<n, 256, 0, st>>>(A, m, lda, out);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+extern "C" {
+
+int dplr_gpu_factor(dplr_gpu_plan plan, int flags, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_factor: null plan");
+    return factor_build(p, flags, (cudaStream_t)stream);
+}
+
+int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int ldb, double *X,
+                   int ldx, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve: null plan");
+    if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1))
+        return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve: invalid n/ldb/ldx");
+    if (B == X) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve: B and X must not alias");
+    int tr = !(trans == 'N' || trans == 'n');
+    return factor_solve(p, tr, n, B, ldb, X, ldx, (cudaStream_t)stream);
+}
+
+int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, double *X, int ldx,
+                           double tol, int maxiter, double *rel_resid, int *iters, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: null plan");
+    if (!p->fact) return fail(DPLR_GPU_ESTATE, "dplr_gpu_solve_refined: plan is not factored");
+    if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1) || maxiter < 0)
+        return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: invalid arguments");
+    if (n == 0 || p->m == 0) {
+        if (rel_resid) *rel_resid = 0.0;
+        if (iters) *iters = 0;
+        return 0;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int m = p->m;
+    // Scratch: residual R, correction D (m x n each), 2n norms.
+    size_t need = (size_t)2 * m * n + 2 * (size_t)n;
+    int rc = ensure_buffer(&p->ybuf, &p->ybuf_doubles, need);
+    if (rc) return rc;
+    double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
+    double *bn = D + (size_t)m * n, *rn = bn + n;
+    std::vector<double> hb(n), hr(n);
+    if ((rc = colnorms_device(B, m, n, ldb, bn, st))) return rc;
+    DG_CUDA(cudaMemcpyAsync(hb.data(), bn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if ((rc = factor_solve(p, 0, n, B, ldb, X, ldx, st))) return rc;
+    double worst = INFINITY;
+    int it = 0;
+    for (;;) {
+        // R = B - A X (FP64 apply of the original matrix)
+        if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
+        if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
+        DG_CUDA(cudaMemcpyAsync(hr.data(), rn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        worst = 0.0;
+        for (int j = 0; j < n; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
+        if (worst <= tol || it >= maxiter) break;
+        if ((rc = factor_solve(p, 0, n, R, m, D, m, st))) return rc;
+        if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
+        ++it;
+    }
+    if (rel_resid) *rel_resid = worst;
+    if (iters) *iters = it;
+    if (!(worst <= tol))
+        return fail(DPLR_GPU_ENOTCONV, "refinement stopped at relative residual %.3e after %d steps",
+                    worst, it);
+    return 0;
+}
+
+int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb, double *X,
+                                int ldx, double tol, int maxiter, double *rel_resid, int *iters,
+                                void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: null plan");
+    if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1))
+        return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: invalid arguments");
+    if (n == 0 || p->m == 0) return dplr_gpu_solve_refined(plan, n, nullptr, 1, nullptr, 1, tol,
+                                                          maxiter, rel_resid, iters, stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t cnt = (size_t)p->m * n;
+    int rc = ensure_buffer(&p->xbuf, &p->xbuf_doubles, 2 * cnt);
+    if (rc) return rc;
+    double *dB = p->xbuf, *dX = p->xbuf + cnt;
+    DG_CUDA(cudaMemcpy2DAsync(dB, sizeof(double) * p->m, B, sizeof(double) * ldb,
+                              sizeof(double) * p->m, n, cudaMemcpyHostToDevice, st));
+    rc = dplr_gpu_solve_refined(plan, n, dB, p->m, dX, p->m, tol, maxiter, rel_resid, iters, stream);
+    if (rc && rc != DPLR_GPU_ENOTCONV) return rc;
+    DG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, dX, sizeof(double) * p->m,
+                              sizeof(double) * p->m, n, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+long long dplr_gpu_factor_device_bytes(dplr_gpu_plan plan)
+{
+    return plan ? factor_bytes((Plan *)plan) : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+"""Device-resident PLR matrices: the Python face of the plan API.
+
+A ``GpuPlan`` owns one ``dplr_gpu_plan`` (block table + factor pool in
+HBM) built from a host tree.  Right-hand sides are torch CUDA tensors of
+shape (n, m), float64, contiguous: row j is column j of the column-major
+m x n block the C ABI sees (leading dimension m).  All calls go through
+libdplr_gb300.so; there is no other code path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native, tree
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream
+
+
+def _check_block(x: torch.Tensor, m: int, name: str) -> None:
+    if not (x.is_cuda and x.dtype == torch.float64 and x.dim() == 2 and x.shape[1] == m
+            and x.is_contiguous()):
+        raise ValueError(f"{name} must be a contiguous CUDA float64 tensor of shape (n, {m})")
+
+
+class GpuPlan:
+    def __init__(self, node_or_cptr, stream=None):
+        lib = _native.lib()
+        self._owned_c = None
+        if isinstance(node_or_cptr, (tree.Dense, tree.HNode)):
+            cptr = tree.to_c(node_or_cptr)
+            self._owned_c = cptr
+        else:
+            cptr = node_or_cptr
+        self.m = int(cptr.contents.size)
+        h = ctypes.c_void_p()
+        _native.check(lib.dplr_gpu_plan_create(self.m, cptr, _stream_ptr(stream), ctypes.byref(h)),
+                      "dplr_gpu_plan_create")
+        self._h = h
+        if self._owned_c is not None:
+            tree.free_c(self._owned_c)
+            self._owned_c = None
+        mm, nnz, lev, mr = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+        lib.dplr_gpu_plan_info(self._h, ctypes.byref(mm), ctypes.byref(nnz), ctypes.byref(lev),
+                               ctypes.byref(mr))
+        self.nnz, self.levels, self.max_rank = nnz.value, lev.value, mr.value
+        self.factored = False
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _native.lib().dplr_gpu_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def device_bytes(self) -> int:
+        lib = _native.lib()
+        return int(lib.dplr_gpu_plan_device_bytes(self._h)) + int(
+            lib.dplr_gpu_factor_device_bytes(self._h))
+
+    # -------------------------------------------------------------- apply
+    def apply(self, x: torch.Tensor, trans: str = "N", alpha: float = 1.0, beta: float = 0.0,
+              out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """out := alpha*op(A) x + beta*out for x of shape (n, m)."""
+        _check_block(x, self.m, "x")
+        if out is None:
+            out = torch.empty_like(x)
+            beta = 0.0
+        _check_block(out, self.m, "out")
+        n = x.shape[0]
+        _native.check(_native.lib().dplr_gpu_apply(self._h, trans.encode(), n, alpha, x.data_ptr(),
+                                                   self.m, beta, out.data_ptr(), self.m,
+                                                   _stream_ptr(stream)), "dplr_gpu_apply")
+        return out
+
+    # -------------------------------------------------------------- solve
+    def factor(self, transposed: bool = False, stream=None) -> None:
+        _native.check(_native.lib().dplr_gpu_factor(self._h, 1 if transposed else 0,
+                                                    _stream_ptr(stream)), "dplr_gpu_factor")
+        self.factored = True
+
+    def solve(self, b: torch.Tensor, trans: str = "N", out: torch.Tensor | None = None,
+              stream=None) -> torch.Tensor:
+        _check_block(b, self.m, "b")
+        out = torch.empty_like(b) if out is None else out
+        _check_block(out, self.m, "out")
+        _native.check(_native.lib().dplr_gpu_solve(self._h, trans.encode(), b.shape[0],
+                                                   b.data_ptr(), self.m, out.data_ptr(), self.m,
+                                                   _stream_ptr(stream)), "dplr_gpu_solve")
+        return out
+
+    def solve_refined(self, b: torch.Tensor, tol: float = 1e-12, maxiter: int = 10,
+                      out: torch.Tensor | None = None, stream=None):
+        """Refined FP64 solve; returns (x, relative residual, corrections)."""
+        _check_block(b, self.m, "b")
+        out = torch.empty_like(b) if out is None else out
+        _check_block(out, self.m, "out")
+        res, its = ctypes.c_double(), ctypes.c_int()
+        rc = _native.lib().dplr_gpu_solve_refined(self._h, b.shape[0], b.data_ptr(), self.m,
+                                                  out.data_ptr(), self.m, tol, maxiter,
+                                                  ctypes.byref(res), ctypes.byref(its),
+                                                  _stream_ptr(stream))
+        _native.check(rc, "dplr_gpu_solve_refined")
+        return out, res.value, its.value

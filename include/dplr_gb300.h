@@ -58,6 +58,47 @@ DPLR_API long long dplr_gpu_plan_device_bytes(dplr_gpu_plan plan);
 DPLR_API int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha, const double *X,
                    int ldx, double beta, double *Y, int ldy, void *stream);
 
+/* Woodbury factorisation of the planned matrix (replaces forming inv(A)
+ * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):
+ * leaf inverses, per-level panels Z = D^-1 W and capacitance inverses
+ * (I + S V~^T Z)^-1, all FP64.  DPLR_GPU_FACTOR_TRANSPOSED also builds
+ * the panels D^-T V~ needed by transposed solves. */
+#define DPLR_GPU_FACTOR_TRANSPOSED 1
+DPLR_API int dplr_gpu_factor(dplr_gpu_plan plan, int flags, void *stream);
+DPLR_API long long dplr_gpu_factor_device_bytes(dplr_gpu_plan plan);
+
+/* X := op(A)^-1 B (device arrays, m x n); B and X must not alias. */
+DPLR_API int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int ldb,
+                            double *X, int ldx, void *stream);
+
+/* X := A^-1 B refined until max_j ||B_j - A X_j|| / ||B_j|| <= tol, the
+ * residual computed by the FP64 apply of A; at most maxiter corrections.
+ * Reports the final relative residual and the number of corrections;
+ * returns DPLR_GPU_ENOTCONV if the tolerance was not reached. */
+DPLR_API int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb,
+                                    double *X, int ldx, double tol, int maxiter,
+                                    double *rel_resid, int *iters, void *stream);
+
+/* The same refined solve with B and X in host memory (column-major,
+ * leading dimensions ldb, ldx >= m): B is copied to the device, solved and
+ * X copied back inside the call (pinned host memory makes the copies
+ * asynchronous DMA). */
+DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb,
+                                         double *X, int ldx, double tol, int maxiter,
+                                         double *rel_resid, int *iters, void *stream);
+
+/* Instrumentation.  dplr_gpu_launch_count: kernels launched by this
+ * library since load.  Between dplr_gpu_profile_start() and
+ * dplr_gpu_profile_stop() the main kernels are bracketed by CUDA events on
+ * their launching stream; stop synchronises and returns the number of
+ * kernel kinds, whose totals (milliseconds, algorithmic flops and bytes,
+ * launches) dplr_gpu_profile_entry() reports. */
+DPLR_API long long dplr_gpu_launch_count(void);
+DPLR_API int dplr_gpu_profile_start(void);
+DPLR_API int dplr_gpu_profile_stop(void);
+DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double *flops,
+                                    double *bytes, int *launches);
+
 /* Associate the drop-in entry points with a plan for this host tree
  * (they then skip the upload).  dplr_gpu_unregister drops the link. */
 DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);

@@ -79,16 +79,20 @@ def replay_pdmm(api, rec: dict, tol: float) -> None:
         tree.free_c(a)
 
 
-def compare_trees(got, want, tol: float, where: str = "", scale: float | None = None) -> None:
+def compare_trees(got, want, tol: float, where: str = "", scale: float | None = None,
+                  sig_tol: float | None = None) -> None:
     """Same structure and ranks; every block's product U diag(sig) V^T and
     every leaf within tol * scale (Frobenius; scale defaults to the norm of
-    the whole matrix); sig entries within tol of the block's largest.
+    the whole matrix); sig entries within sig_tol (default: tol) of the
+    block's largest.
 
     Factor columns are compared through their products because columns
     whose singular value is negligible point in directions set by
     rounding, which differ between BLAS implementations."""
     if scale is None:
         scale = float(np.linalg.norm(tree.to_dense(want)))
+    if sig_tol is None:
+        sig_tol = tol
     assert type(got) is type(want), f"{where}: node type differs"
     if isinstance(want, tree.Dense):
         err = float(np.linalg.norm(got.d - want.d))
@@ -102,10 +106,10 @@ def compare_trees(got, want, tol: float, where: str = "", scale: float | None = 
             assert err <= tol * scale, f"{where}: block err {err / scale}"
             smax = float(np.max(np.abs(want.sig)))
             serr = float(np.max(np.abs(got.sig - want.sig)))
-            assert serr <= tol * max(smax, 1e-300) + 1e-300, f"{where}: sig err {serr / smax}"
+            assert serr <= sig_tol * max(smax, 1e-300) + 1e-300, f"{where}: sig err {serr / smax}"
     else:
         for q in ("nw", "ne", "se", "sw"):
-            compare_trees(getattr(got, q), getattr(want, q), tol, where + "." + q, scale)
+            compare_trees(getattr(got, q), getattr(want, q), tol, where + "." + q, scale, sig_tol)
 
 
 def replay_prk(api, rec: dict, tol: float) -> None:
@@ -127,7 +131,7 @@ def replay_prk(api, rec: dict, tol: float) -> None:
         i += 1
 
 
-def replay_inv(api, rec: dict, tol: float, dense_tol: float) -> None:
+def replay_inv(api, rec: dict, tol: float, dense_tol: float, sig_tol: float | None = None) -> None:
     t = matrix(rec)
     m = t.size
     i = 0
@@ -145,5 +149,5 @@ def replay_inv(api, rec: dict, tol: float, dense_tol: float) -> None:
         want = tree.unflatten(rec[f"inv{i}_meta"], rec[f"inv{i}_data"])
         e = rel_err(tree.to_dense(got), tree.to_dense(want))
         assert e <= dense_tol, f"inv{i}: dense rel err {e}"
-        compare_trees(got, want, tol, f"inv{i}")
+        compare_trees(got, want, tol, f"inv{i}", sig_tol=sig_tol)
         i += 1

@@ -73,4 +73,4 @@ def test_gpu_inverse_matches_golden(path):
     api = _native.api()
     if not api.has("geinv"):
         pytest.skip("dplrgeinv not in this build")
-    golden_io.replay_inv(api, golden_io.load(path), tol=1e-8, dense_tol=1e-11)
+    golden_io.replay_inv(api, golden_io.load(path), tol=1e-12, dense_tol=1e-11, sig_tol=1e-10)
