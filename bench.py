@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the PLR solve path: RHS/s at N = 2^18 with 256 right-hand sides.
+
+Workload (the mixed-precision configuration of the reference's target):
+N = 262144 points uniform in the unit square, ordered by kd-tree bisection,
+Gaussian kernel exp(-r^2 / (2 * 0.05^2)) + 1e-2 * I, leaf 256 (10 levels),
+adaptive off-diagonal ranks (tol 1e-10, clamped to [8, 128]), 256
+standard-normal right-hand sides; a step is one solve of all 256 right-hand
+sides refined to relative residual <= 1e-12 (max over columns), the
+residual computed by the FP64 PLR apply of the matrix.
+
+Arms:
+  --impl ours       libdplr_gb300.so: Woodbury factorisation on the GPU
+                    (setup, untimed), then timed refined solves.
+  --impl reference  the reference algorithm on the host cores: the explicit
+                    PLR inverse (dplrgeinv) applied with dplrgepdmm and
+                    refined with dplrgepdmm of the matrix, run by the CPU
+                    oracle (the reference's C restated, linked to an
+                    optimised BLAS, all host threads) on a bounded sample.
+
+Prints one JSON line (rank 0).  Under torchrun each rank solves its own
+replica (the path does not shard: replicas only) and the value is the
+aggregate over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("PLR solve RHS/s @N=2^18,256 RHS: mixed+refined vs FP64 GPU at ≤1e-12 rel resid")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1 << 18)
+    ap.add_argument("--leaf", type=int, default=256)
+    ap.add_argument("--rhs", type=int, default=256)
+    ap.add_argument("--rmax", type=int, default=128)
+    ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--maxiter", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 14,
+                    help="size of the diagonal sub-block the CPU baseline runs on")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock, power and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v == "Active"})
+        clocks = sorted(r[0] for r in rows)
+        return {"sm_mhz": clocks[len(clocks) // 2], "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def workload_config(args, stats=None, extra=None) -> dict:
+    cfg = {
+        "workload": (f"2D Gaussian kernel PLR solve, N={args.n}, leaf {args.leaf}, "
+                     f"{args.rhs} RHS, refined to {args.tol:g}"),
+        "n": args.n, "leaf": args.leaf, "levels": 0, "rhs": args.rhs,
+        "kernel": "exp(-r^2/(2*0.05^2)) + 1e-2*I on uniform unit-square points, kd-tree order",
+        "ranks": "adaptive, tol 1e-10, clamped to [8, %d]" % args.rmax,
+        "tol": args.tol, "seed": args.seed,
+        "l2": "inputs larger than L2 (factors several GB)",
+    }
+    if stats is not None:
+        cfg["ranks_by_level"] = stats.ranks
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def build_matrix(args, device="cuda"):
+    from dplr_gb300 import gen_gpu
+    stats = gen_gpu.GenStats()
+    t = gen_gpu.kernel_tree_2d(n=args.n, leaf=args.leaf, rmax=args.rmax, seed=args.seed,
+                               device=device, stats=stats)
+    return t, stats
+
+
+# --------------------------------------------------------------- CPU sample
+
+def cpu_sample(t, args, threads: int):
+    """The reference algorithm (explicit inverse + inverse apply + refinement
+    by the forward apply) on a diagonal sub-block of the matrix, on the host
+    cores; returns RHS/s scaled to the full matrix by the flop ratio."""
+    import numpy as np
+
+    from dplr_gb300 import tree as tr
+    from oracle import pyoracle
+    orc = pyoracle.oracle("best")
+    pyoracle.set_threads(orc, threads)
+    sub = t
+    while sub.size > args.cpu_sample and isinstance(sub, tr.HNode):
+        sub = sub.nw
+    m = sub.size
+    a = tr.to_c(sub)
+    b_inv = tr.new_empty()
+    t0 = time.time()
+    info = orc.geinv(m, a, b_inv, 0.0)
+    t_inv = time.time() - t0
+    if info != 0:
+        raise RuntimeError(f"oracle geinv failed: {info}")
+    nnz_a, nnz_b = orc.nz(m, a), orc.nz(m, b_inv)
+    nrhs = args.rhs
+    rng = np.random.default_rng(args.seed + 7)
+    bvec = rng.standard_normal(m * nrhs)
+    x = np.zeros(m * nrhs)
+    r = np.empty(m * nrhs)
+    d = np.empty(m * nrhs)
+    t0 = time.time()
+    orc.gepdmm("N", "N", m, nrhs, 1.0, b_inv, bvec, m, 0.0, x, m)
+    its, res = 0, np.inf
+    bn = np.linalg.norm(bvec.reshape(nrhs, m), axis=1)
+    while True:
+        r[:] = bvec
+        orc.gepdmm("N", "N", m, nrhs, -1.0, a, x, m, 1.0, r, m)
+        res = float(np.max(np.linalg.norm(r.reshape(nrhs, m), axis=1) / bn))
+        if res <= args.tol or its >= args.maxiter:
+            break
+        orc.gepdmm("N", "N", m, nrhs, 1.0, b_inv, r, m, 0.0, d, m)
+        x += d
+        its += 1
+    t_solve = time.time() - t0
+    tr.free_c(a)
+    tr.free_c(b_inv)
+    work_sample = (2.0 * nnz_b + 2.0 * nnz_a) * (its + 1)
+    nnz_a_full = tr.nnz(t)
+    nnz_b_full = inverse_nnz(t)
+    work_full = (2.0 * nnz_b_full + 2.0 * nnz_a_full) * (its + 1)
+    rhs_s_sample = nrhs / t_solve
+    return {
+        "value": rhs_s_sample * work_sample / work_full,
+        "rhs_per_s_sample": rhs_s_sample,
+        "sample_n": m, "sample_inverse_s": t_inv, "sample_solve_s": t_solve,
+        "sample_iters": its, "sample_resid": res, "nnz_inverse_full": nnz_b_full,
+        "blas_optimised": bool(pyoracle.oracle("best").lib.orc_blas_optimised()),
+    }
+
+
+def inverse_nnz(t) -> int:
+    """dplrnz of DPLR's explicit inverse: every block keeps its own rank and
+    gains the rank of each ancestor's correction on its side."""
+    from dplr_gb300 import tree as tr
+
+    def walk(node, extra_ne_sw):
+        if isinstance(node, tr.Dense):
+            return node.size * node.size
+        h = node.size // 2
+        r1, r2 = node.ne.rank, node.sw.rank
+        tot = node.size * (r1 + r2 + 2 * extra_ne_sw)
+        return tot + walk(node.nw, extra_ne_sw + r2) + walk(node.se, extra_ne_sw + r1)
+
+    return walk(t, 0)
+
+
+# --------------------------------------------------------------------- arms
+
+def run_reference(args):
+    world, rank, local = dist_init()
+    if rank != 0:
+        return
+    import numpy as np  # noqa: F401
+    torch_ok = True
+    try:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+    except Exception:
+        torch_ok = False
+        dev = "cpu"
+    if not torch_ok:
+        print(json.dumps({"impl": "reference", "unavailable": "torch missing for input generation"}))
+        return
+    t, stats = build_matrix(args, device=dev)
+    threads = os.cpu_count() or 1
+    steps = []
+    for _ in range(max(1, args.steps)):
+        steps.append(cpu_sample(t, args, threads))
+    vals = [s["value"] for s in steps]
+    value = sorted(vals)[len(vals) // 2]
+    sample = (f"reference algorithm (explicit inverse by dplrgeinv, applied by dplrgepdmm, refined "
+              f"with dplrgepdmm of A) on the leading {steps[0]['sample_n']}x{steps[0]['sample_n']} "
+              f"diagonal sub-block, {args.rhs} RHS; RHS/s scaled to N={args.n} by the ratio of "
+              f"solve flops (2*nnz(inv)+2*nnz(A) per refinement step)")
+    out = {
+        "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": 1, "steps": len(steps),
+        "warmup": 0, "ms_per_step": 1000.0 * args.rhs / value if value else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": workload_config(args, stats, {"parallelism": "host cores"}),
+        "cpu_baseline": {"value": value, "unit": "RHS/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "detail": steps[0],
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+
+    t, stats = build_matrix(args, device=str(device))
+    t_gen = stats.seconds
+    t0 = time.time()
+    plan = GpuPlan(t)
+    t_upload = time.time() - t0
+    torch.cuda.synchronize()
+    t0 = time.time()
+    plan.factor()
+    torch.cuda.synchronize()
+    t_factor = time.time() - t0
+
+    g = torch.Generator(device=device)
+    g.manual_seed(args.seed + 1000 * rank + 3)
+    B = torch.randn(args.rhs, args.n, dtype=torch.float64, device=device, generator=g)
+    X = torch.empty_like(B)
+    stream = torch.cuda.current_stream(device)
+
+    for _ in range(max(3, args.warmup)):
+        plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X, strict=False)
+    torch.cuda.synchronize()
+
+    # ---------------- timed region: device-resident inputs
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    _native.profile_start()
+    l0 = _native.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    resid, iters = [], []
+    for _ in range(args.steps):
+        _, res, its = plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X,
+                                         strict=False)
+        resid.append(res)
+        iters.append(its)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = _native.launch_count() - l0
+    prof = _native.profile_stop()
+    clocks = sampler.stop()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(ms, world, device)
+    value = args.rhs * args.steps * world / (ms_max / 1000.0)
+
+    # ---------------- end to end: host buffers through the C ABI
+    import ctypes
+    Bh = B.cpu().pin_memory()
+    Xh = torch.empty_like(Bh).pin_memory()
+    lib = _native.lib()
+    res_c, its_c = ctypes.c_double(), ctypes.c_int()
+
+    def e2e_step():
+        rc = lib.dplr_gpu_solve_refined_host(plan.handle, args.rhs, Bh.data_ptr(), args.n,
+                                             Xh.data_ptr(), args.n, args.tol, args.maxiter,
+                                             ctypes.byref(res_c), ctypes.byref(its_c),
+                                             stream.cuda_stream)
+        if rc != -5:
+            _native.check(rc, "dplr_gpu_solve_refined_host")
+
+    e2e_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, device)
+    e2e_value = args.rhs * args.steps * world / e2e_s
+    nbytes = args.rhs * args.n * 8
+
+    # ---------------- roofline of the dominant kernel
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (kms, kfl, kby, kla) = dom
+    tflops = kfl / (kms / 1000.0) / 1e12
+    gbs = kby / (kms / 1000.0) / 1e9
+    fp64_peak = 1.19  # TFLOP/s, DFMA throughput probe on this GB300 (profiles/fp64_peak.md)
+    roofline = {"kernel": name, "bound": "fp64", "achieved": tflops, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": tflops / fp64_peak, "traffic": None,
+                "algorithmic_gbs": gbs, "share_of_timed": kms / ms,
+                "peak_source": "measured DFMA probe (not in MEASURED_PEAKS.json)"}
+    kernels = {k: {"ms": v[0], "tflops": v[1] / (v[0] / 1e3) / 1e12 if v[0] else 0.0,
+                   "gbs": v[2] / (v[0] / 1e3) / 1e9 if v[0] else 0.0, "launches": v[3]}
+               for k, v in prof.items()}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": workload_config(args, stats, {
+            "levels": plan.levels, "nnz": plan.nnz, "precision": "fp64 (Woodbury, FP64 refinement)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "setup_s": {"generate": t_gen, "upload": t_upload, "factor": t_factor},
+            "refinement_iters": iters, "final_rel_resid": resid,
+            "converged": all(r <= args.tol for r in resid)}),
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "RHS/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "kernels": kernels,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cb = cpu_sample(t, args, os.cpu_count() or 1)
+            out["cpu_baseline"] = {
+                "value": cb["value"], "unit": "RHS/s", "cores": os.cpu_count() or 1, "kind": "port",
+                "sample": (f"oracle (reference algorithm restated, optimised BLAS) on the leading "
+                           f"{cb['sample_n']} diagonal sub-block; explicit inverse + apply + "
+                           f"refinement, {args.rhs} RHS, scaled to N={args.n} by solve flops"),
+                "detail": cb}
+        except Exception as exc:  # the baseline must not hide the GPU result
+            out["cpu_baseline"] = {"value": None, "unit": "RHS/s", "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(out))
+    plan.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

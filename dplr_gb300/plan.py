@@ -102,8 +102,9 @@ class GpuPlan:
         return out
 
     def solve_refined(self, b: torch.Tensor, tol: float = 1e-12, maxiter: int = 10,
-                      out: torch.Tensor | None = None, stream=None):
-        """Refined FP64 solve; returns (x, relative residual, corrections)."""
+                      out: torch.Tensor | None = None, stream=None, strict: bool = True):
+        """Refined FP64 solve; returns (x, relative residual, corrections).
+        With strict=False a solve that stops above `tol` is returned too."""
         _check_block(b, self.m, "b")
         out = torch.empty_like(b) if out is None else out
         _check_block(out, self.m, "out")
@@ -112,5 +113,6 @@ class GpuPlan:
                                                   out.data_ptr(), self.m, tol, maxiter,
                                                   ctypes.byref(res), ctypes.byref(its),
                                                   _stream_ptr(stream))
-        _native.check(rc, "dplr_gpu_solve_refined")
+        if rc != -5 or strict:
+            _native.check(rc, "dplr_gpu_solve_refined")
         return out, res.value, its.value
