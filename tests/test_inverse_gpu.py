@@ -58,7 +58,7 @@ def test_geinv_matches_oracle(name, eps):
     # operator parity at 1e-12 of the inverse's norm; individual singular
     # values are an intermediate of two different rounding paths (DPLR
     # inverts X = S^-1 K, the GPU K), so they are held to 1e-10
-    golden_io.compare_trees(bg, bo, 1e-12, sig_tol=1e-10)
+    golden_io.compare_trees(bg, bo, 1e-12, sig_tol=1e-10, allow=2.0 * eps)
     if eps == 0.0:
         d = tree.to_dense(t)
         inv = tree.to_dense(bg)
