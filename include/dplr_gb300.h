@@ -79,6 +79,21 @@ DPLR_API int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, 
                                     double *X, int ldx, double tol, int maxiter,
                                     double *rel_resid, int *iters, void *stream);
 
+/* Y := alpha*op(A)*X + beta*Y like dplr_gpu_apply, but without allocating
+ * any device memory.  No counterpart in DPLR (whose routines malloc per
+ * block visit).  For callers that cannot allocate when they apply: code
+ * recorded by CUDA stream capture, latency-critical paths that must avoid
+ * cudaMalloc/cudaFree and their implicit synchronisation, and hosts that
+ * fix the library's device memory in advance.  Scratch is a static 64 MiB
+ * device array shared by all calls on a device: calls that may overlap on
+ * the GPU race and must be ordered by the caller; a call needing more
+ * scratch than that, (sum of ranks + partial panels) * n doubles, fails
+ * with DPLR_GPU_EINVAL.  The first call on a device resolves the array's
+ * address and should come before any stream capture. */
+DPLR_API int dplr_gpu_apply_noalloc(dplr_gpu_plan plan, char trans, int n, double alpha,
+                                    const double *X, int ldx, double beta, double *Y, int ldy,
+                                    void *stream);
+
 /* The same refined solve with B and X in host memory (column-major,
  * leading dimensions ldb, ldx >= m): B is copied to the device, solved and
  * X copied back inside the call (pinned host memory makes the copies
