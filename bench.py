@@ -51,6 +51,12 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--maxiter", type=int, default=8)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
+                    help="inner solver of the refinement: sliced tensor-core sweep or FP64 sweep")
+    ap.add_argument("--mixed-slices", type=int, default=6,
+                    help="bf16 slices of the mixed inner solve (3 to 6)")
+    ap.add_argument("--residual", choices=["sliced", "fp64"], default="sliced",
+                    help="refinement residual: exact-slice tensor-core products or the FP64 apply")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-sample", type=int, default=1 << 14,
                     help="size of the diagonal sub-block the CPU baseline runs on")
@@ -300,41 +306,81 @@ def run_ours(args):
     plan.factor()
     torch.cuda.synchronize()
     t_factor = time.time() - t0
+    precise = args.residual == "sliced"
+    t0 = time.time()
+    if precise:
+        plan.prepare_sliced()
+    torch.cuda.synchronize()
+    t_slice = time.time() - t0
 
     g = torch.Generator(device=device)
     g.manual_seed(args.seed + 1000 * rank + 3)
     B = torch.randn(args.rhs, args.n, dtype=torch.float64, device=device, generator=g)
     X = torch.empty_like(B)
     stream = torch.cuda.current_stream(device)
+    mixed = args.precision == "mixed"
+    t0 = time.time()
+    if mixed:
+        plan.prepare_mixed(args.mixed_slices)
+    torch.cuda.synchronize()
+    t_mixed = time.time() - t0
 
-    for _ in range(max(3, args.warmup)):
-        plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X, strict=False)
-    torch.cuda.synchronize()
+    def run_steps(use_mixed, steps, profile=False):
+        """Warm up, then time `steps` refined solves; returns timing and stats."""
+        for _ in range(max(3, args.warmup)):
+            plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X, strict=False,
+                               precise=precise, mixed=use_mixed)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if profile else None
+        if profile:
+            sampler.start()
+            _native.profile_start()
+        l0 = _native.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        resid, iters = [], []
+        for _ in range(steps):
+            _, res, its = plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X,
+                                             strict=False, precise=precise, mixed=use_mixed)
+            resid.append(res)
+            iters.append(its)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out = {"launches": _native.launch_count() - l0, "resid": resid, "iters": iters}
+        if profile:
+            out["prof"] = _native.profile_stop()
+            out["clocks"] = sampler.stop()
+        barrier(world)
+        ms = e0.elapsed_time(e1)
+        out["ms"] = max_over_ranks(ms, world, device)
+        return out
 
-    # ---------------- timed region: device-resident inputs
-    barrier(world)
-    torch.cuda.synchronize()
-    sampler = ClockSampler(local)
-    sampler.start()
-    _native.profile_start()
-    l0 = _native.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    resid, iters = [], []
-    for _ in range(args.steps):
-        _, res, its = plan.solve_refined(B, tol=args.tol, maxiter=args.maxiter, out=X,
-                                         strict=False)
-        resid.append(res)
-        iters.append(its)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    launches = _native.launch_count() - l0
-    prof = _native.profile_stop()
-    clocks = sampler.stop()
-    barrier(world)
-    ms = e0.elapsed_time(e1)
-    ms_max = max_over_ranks(ms, world, device)
+    # ---------------- timed region: device-resident inputs (headline path)
+    head = run_steps(mixed, args.steps, profile=True)
+    ms_max = head["ms"]
     value = args.rhs * args.steps * world / (ms_max / 1000.0)
+    prof, clocks, launches = head["prof"], head["clocks"], head["launches"]
+    resid, iters = head["resid"], head["iters"]
+    ms = ms_max
+    # ---------------- the plain FP64 GPU solve (FP64 Woodbury sweeps), same residual
+    fp64 = run_steps(False, args.steps) if mixed else head
+    fp64_value = args.rhs * args.steps * world / (fp64["ms"] / 1000.0)
+    # ---------------- one unrefined FP64 Woodbury solve (does not reach the tolerance)
+    for _ in range(3):
+        plan.solve(B, out=X)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(args.steps):
+        plan.solve(B, out=X)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = max_over_ranks(p0.elapsed_time(p1), world, device)
+    R = plan.residual(X, B, precise=precise)
+    plain_res = float((R.norm(dim=1) / B.norm(dim=1)).max())
+    del R
 
     # ---------------- end to end: host buffers through the C ABI
     import ctypes
@@ -346,6 +392,7 @@ def run_ours(args):
     def e2e_step():
         rc = lib.dplr_gpu_solve_refined_host(plan.handle, args.rhs, Bh.data_ptr(), args.n,
                                              Xh.data_ptr(), args.n, args.tol, args.maxiter,
+                                             (1 if precise else 0) | (2 if mixed else 0),
                                              ctypes.byref(res_c), ctypes.byref(its_c),
                                              stream.cuda_stream)
         if rc != -5:
@@ -368,10 +415,22 @@ def run_ours(args):
     tflops = kfl / (kms / 1000.0) / 1e12
     gbs = kby / (kms / 1000.0) / 1e9
     fp64_peak = 1.19  # TFLOP/s, DFMA throughput probe on this GB300 (profiles/fp64_peak.md)
-    roofline = {"kernel": name, "bound": "fp64", "achieved": tflops, "peak": fp64_peak,
-                "unit": "TFLOP/s", "frac": tflops / fp64_peak, "traffic": None,
-                "algorithmic_gbs": gbs, "share_of_timed": kms / ms,
-                "peak_source": "measured DFMA probe (not in MEASURED_PEAKS.json)"}
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        peaks = json.load(open(peaks_path))
+        bf16_peak, peak_src = float(peaks["bf16_tflops_sustained"]), "of measured (sustained bf16)"
+    except Exception:
+        bf16_peak, peak_src = 1700.0, "of fallback (sustained bf16)"
+    if name.startswith(("sliced_", "mixed_")):
+        roofline = {"kernel": name, "bound": "tensor", "achieved": tflops, "peak": bf16_peak,
+                    "unit": "TFLOP/s", "frac": tflops / bf16_peak, "traffic": None,
+                    "algorithmic_gbs": gbs, "share_of_timed": kms / ms, "peak_source": peak_src,
+                    "note": "bf16 MMA flops of all slice pairs (mma.sync m16n8k16)"}
+    else:
+        roofline = {"kernel": name, "bound": "fp64", "achieved": tflops, "peak": fp64_peak,
+                    "unit": "TFLOP/s", "frac": tflops / fp64_peak, "traffic": None,
+                    "algorithmic_gbs": gbs, "share_of_timed": kms / ms,
+                    "peak_source": "measured DFMA probe (profiles/fp64_peak.md)"}
     kernels = {k: {"ms": v[0], "tflops": v[1] / (v[0] / 1e3) / 1e12 if v[0] else 0.0,
                    "gbs": v[2] / (v[0] / 1e3) / 1e9 if v[0] else 0.0, "launches": v[3]}
                for k, v in prof.items()}
@@ -379,12 +438,27 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_max / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+bf16" if mixed else "f64",
         "data": "synthetic",
         "config": workload_config(args, stats, {
-            "levels": plan.levels, "nnz": plan.nnz, "precision": "fp64 (Woodbury, FP64 refinement)",
+            "levels": plan.levels, "nnz": plan.nnz,
+            "precision": ((f"mixed: {args.mixed_slices}-slice bf16 Woodbury inner solves (tensor "
+                           "cores, FP64 capacitance), " if mixed else "fp64 Woodbury inner solves, ") +
+                          ("residual from 8 exact bf16 slices with double-double accumulation"
+                           if precise else "FP64 residual")),
             "parallelism": "replicas" if world > 1 else "single GPU",
-            "setup_s": {"generate": t_gen, "upload": t_upload, "factor": t_factor},
+            "setup_s": {"generate": t_gen, "upload": t_upload, "factor": t_factor,
+                        "slice": t_slice, "mixed_slices": t_mixed},
+            "fp64_gpu_solve": {"value": fp64_value, "unit": "RHS/s",
+                               "ms_per_step": fp64["ms"] / args.steps,
+                               "refinement_iters": fp64["iters"],
+                               "final_rel_resid": fp64["resid"],
+                               "converged": all(r <= args.tol for r in fp64["resid"])},
+            "fp64_plain_solve": {"value": args.rhs * args.steps * world / (plain_ms / 1000.0),
+                                 "unit": "RHS/s", "ms_per_step": plain_ms / args.steps,
+                                 "rel_resid": plain_res,
+                                 "note": "one FP64 Woodbury sweep without refinement"},
             "refinement_iters": iters, "final_rel_resid": resid,
             "converged": all(r <= args.tol for r in resid)}),
         "clocks": clocks,

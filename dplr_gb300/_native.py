@@ -44,11 +44,15 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("dplr_gpu_solve", c_int, [c_void_p, c_char, c_int, c_void_p, c_int, c_void_p, c_int,
                                   c_void_p])
     sig("dplr_gpu_solve_refined", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
-                                          c_double, c_int, POINTER(c_double), POINTER(c_int),
-                                          c_void_p])
+                                          c_double, c_int, c_int, POINTER(c_double),
+                                          POINTER(c_int), c_void_p])
+    sig("dplr_gpu_prepare_sliced", c_int, [c_void_p, c_void_p])
+    sig("dplr_gpu_prepare_mixed", c_int, [c_void_p, c_int, c_void_p])
+    sig("dplr_gpu_residual", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                     c_int, c_int, c_void_p])
     sig("dplr_gpu_solve_refined_host", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
-                                               c_double, c_int, POINTER(c_double), POINTER(c_int),
-                                               c_void_p])
+                                               c_double, c_int, c_int, POINTER(c_double),
+                                               POINTER(c_int), c_void_p])
     sig("dplr_gpu_launch_count", c_longlong, [])
     sig("dplr_gpu_profile_start", c_int, [])
     sig("dplr_gpu_profile_stop", c_int, [])

@@ -144,6 +144,10 @@ struct Plan {
     long long device_bytes = 0;
     // Woodbury factorisation (filled by factor.cu)
     void *fact = nullptr;
+    // exact-slice factor copies (sliced.cu)
+    void *sliced = nullptr;
+    // low-precision sliced solve (sliced.cu)
+    void *mixed = nullptr;
 };
 
 // plan.cu

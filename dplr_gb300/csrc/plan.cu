@@ -371,11 +371,15 @@ void free_schedule(Schedule &S)
 }
 
 void factor_free(Plan *p);   // factor.cu
+void sliced_free(Plan *p);   // sliced.cu
+void mixed_free(Plan *p);    // sliced.cu
 
 void plan_free(Plan *p)
 {
     if (!p) return;
+    mixed_free(p);
     factor_free(p);
+    sliced_free(p);
     cudaFree(p->pool);
     cudaFree(p->d_lr);
     cudaFree(p->d_leaves);

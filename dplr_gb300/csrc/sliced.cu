@@ -1,0 +1,1244 @@
+// sliced.cu -- exact-slice bf16 tensor-core products for the PLR apply.
+//
+// R = B - A X computed with every factor and X cut into 8 bf16 slices of
+// 7 bits (sliced.cuh explains the representation).  The three phases of
+// the FP64 apply (panel, reduce, expand) keep their structure; the inner
+// products become sums over slice pairs (p, q), p + q <= D, of bf16 MMAs
+// (mma.sync m16n8k16, FP32 accumulate).  Per 64-row stage and per slice
+// diagonal d = p + q the FP32 accumulator holds an exact integer, which is
+// shifted by 7 (D - d) and added into a 128-bit integer per output.  The
+// panel's 128-bit partials are summed exactly, converted to double-double
+// and scaled by sig; the expand converts each term to double-double and
+// adds terms with error-free two-sums, so the only roundings are the slice
+// truncation (below 2^-57 of the row/column scale) and double-double
+// arithmetic (2^-106).  That is what lets iterative refinement reach a
+// 1e-12 relative residual where an FP64 residual stalls.
+#include "sliced.cuh"
+#include "factor.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+
+namespace dg {
+
+constexpr int SK = 64;          // inner-dimension rows per stage
+constexpr int SLD = SK + 8;     // padded smem row (bf16 elements)
+constexpr int ST = 64;          // output tile (rows x rhs) of one CTA
+constexpr int kSThreads = 256;
+
+// ------------------------------------------------------------- helpers
+
+__device__ __forceinline__ uint32_t ld32(const bf16 *p)
+{
+    return *reinterpret_cast<const uint32_t *>(p);
+}
+
+// 16-byte global -> shared copy; zero fill when !valid (src is not read).
+__device__ __forceinline__ void cp16(void *smem_dst, const void *gmem_src, bool valid)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    const int sz = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem_src), "r"(sz));
+}
+
+__device__ __forceinline__ void cp_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, const uint32_t *b)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Exponent e with |x| < 2^e for every x of magnitude <= amax (0 for amax 0).
+__device__ __forceinline__ int scale_exp(double amax)
+{
+    return amax > 0.0 ? ilogb(amax) + 1 : 0;
+}
+
+// Slices of y, |y| < 1: a_1 = rint(128 y), then the remainder, 7 bits a slice.
+template <int NS>
+__device__ __forceinline__ void slice_d(double y, bf16 *out, long long stride)
+{
+#pragma unroll
+    for (int p = 0; p < NS; ++p) {
+        double t = y * 128.0;
+        double a = rint(t);
+        y = t - a;                       // exact
+        out[p * stride] = __double2bfloat16(a);
+    }
+}
+
+// Same for a double-double y = hi + lo (|y| < 1).
+template <int NS>
+__device__ __forceinline__ void slice_dd(double hi, double lo, bf16 *out, long long stride)
+{
+#pragma unroll
+    for (int p = 0; p < NS; ++p) {
+        double th = hi * 128.0, tl = lo * 128.0;
+        double a = rint(th);
+        double r = th - a;               // exact
+        double s = r + tl;               // two-sum (r, tl)
+        double bb = s - r;
+        double e = (r - (s - bb)) + (tl - bb);
+        hi = s;
+        lo = e;
+        out[p * stride] = __double2bfloat16(a);
+    }
+}
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
+{
+    s = a + b;
+    double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// 128-bit integer -> double-double (exact split of the top 106 bits).
+__device__ __forceinline__ void i128_to_dd(__int128 w, double &hi, double &lo)
+{
+    hi = (double)w;
+    lo = (double)(w - (__int128)hi);
+}
+
+// One warp: 32 x 16 output block (2 x 2 fragments) for one slice pair over
+// one SK-row stage; As rows are output rows (m), Bs rows are output columns.
+__device__ __forceinline__ void warp_pair(float (&acc)[2][2][4], const bf16 *As, const bf16 *Bs,
+                                          int m0, int n0, int lane)
+{
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < SK; ks += 16) {
+        uint32_t a[2][4], b[2][2];
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm) {
+            const bf16 *r0 = As + (m0 + fm * 16 + g) * SLD + ks + 2 * t;
+            const bf16 *r1 = r0 + 8 * SLD;
+            a[fm][0] = ld32(r0);
+            a[fm][1] = ld32(r1);
+            a[fm][2] = ld32(r0 + 8);
+            a[fm][3] = ld32(r1 + 8);
+        }
+#pragma unroll
+        for (int fn = 0; fn < 2; ++fn) {
+            const bf16 *c0 = Bs + (n0 + fn * 8 + g) * SLD + ks + 2 * t;
+            b[fn][0] = ld32(c0);
+            b[fn][1] = ld32(c0 + 8);
+        }
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn) mma16816(acc[fm][fn], a[fm], b[fn]);
+    }
+}
+
+// All slice pairs of one stage, diagonal by diagonal, flushed exactly.
+template <int NSA, int NSB, int DMAX>
+__device__ __forceinline__ void stage_products(__int128 (&W)[2][2][4], const bf16 *As,
+                                               const bf16 *Bs, int m0, int n0, int lane)
+{
+#pragma unroll 1
+    for (int d = 2; d <= DMAX; ++d) {
+        float acc[2][2][4];
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[fm][fn][i] = 0.0f;
+        const int plo = d - NSB > 1 ? d - NSB : 1, phi = d - 1 < NSA ? d - 1 : NSA;
+#pragma unroll 1
+        for (int p = plo; p <= phi; ++p)
+            warp_pair(acc, As + (p - 1) * ST * SLD, Bs + (d - p - 1) * ST * SLD, m0, n0, lane);
+        const int sh = 7 * (DMAX - d);
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    W[fm][fn][i] += ((__int128)__float2ll_rn(acc[fm][fn][i])) << sh;
+    }
+}
+
+// ----------------------------------------------------------- slicing kernels
+
+struct SliceJob {
+    long long off;     // source element offset of the matrix (column-major, ld)
+    long long doff;    // destination element offset (column-major, same ld)
+    int ld, rows, cols;
+    int exp;           // offset of the exponents
+};
+
+// Column slicing (one exponent per column): one CTA per (job, column).
+template <int NS>
+__global__ void slice_cols_kernel(const SliceJob *jobs, const int *col_base, int njobs,
+                                  const double *src, bf16 *dst, long long stride, int *exps)
+{
+    __shared__ double red[256];
+    // locate job: col_base is the prefix of columns over jobs
+    const int gc = blockIdx.x;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) / 2;
+        if (col_base[mid] <= gc) lo = mid; else hi = mid - 1;
+    }
+    const SliceJob J = jobs[lo];
+    const int c = gc - col_base[lo];
+    const double *col = src + J.off + (long long)c * J.ld;
+    double m = 0.0;
+    for (int i = threadIdx.x; i < J.rows; i += blockDim.x) m = fmax(m, fabs(col[i]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + k]);
+        __syncthreads();
+    }
+    const int e = scale_exp(red[0]);
+    if (threadIdx.x == 0) exps[J.exp + c] = e;
+    for (int i = threadIdx.x; i < J.rows; i += blockDim.x) {
+        long long o = J.doff + (long long)c * J.ld + i;
+        slice_d<NS>(ldexp(col[i], -e), dst + o, stride);
+    }
+}
+
+// Row slicing (one exponent per row): one thread per (job, row); the
+// slices are written row-major with row stride `dld` (>= cols, multiple
+// of 8, zero padded) starting at element `doff` of the job.
+struct RowSliceJob {
+    long long off;     // source element offset (column-major, ld)
+    long long doff;    // destination element offset (row-major, stride dld)
+    int ld, rows, cols, dld;
+    int exp;
+};
+
+template <int NS>
+__global__ void slice_rows_kernel(const RowSliceJob *jobs, const int *row_base, int njobs, int total,
+                                  const double *src, bf16 *dst, long long stride, int *exps)
+{
+    const int gr = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gr >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) / 2;
+        if (row_base[mid] <= gr) lo = mid; else hi = mid - 1;
+    }
+    const RowSliceJob J = jobs[lo];
+    const int r = gr - row_base[lo];
+    double m = 0.0;
+    for (int k = 0; k < J.cols; ++k) m = fmax(m, fabs(src[J.off + r + (long long)k * J.ld]));
+    const int e = scale_exp(m);
+    exps[J.exp + r] = e;
+    const bf16 zero = __float2bfloat16(0.0f);
+    for (int k = 0; k < J.dld; ++k) {
+        bf16 *o = dst + J.doff + (long long)r * J.dld + k;
+        if (k < J.cols) {
+            slice_d<NS>(ldexp(src[J.off + r + (long long)k * J.ld], -e), o, stride);
+        } else {
+#pragma unroll
+            for (int p = 0; p < NS; ++p) o[p * stride] = zero;
+        }
+    }
+}
+
+// Right-hand sides: one exponent per column over all rows.
+__global__ void xcol_exp_kernel(const double *X, int m, int ldx, int *xexp)
+{
+    __shared__ double red[512];
+    const double *col = X + (long long)blockIdx.x * ldx;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) v = fmax(v, fabs(col[i]));
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + k]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) xexp[blockIdx.x] = scale_exp(red[0]);
+}
+
+template <int NS>
+__global__ void xslice_kernel(const double *X, int m, int ldx, int nrhs, const int *xexp, bf16 *xs,
+                              long long stride)
+{
+    const long long cnt = (long long)m * nrhs;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % m), j = (int)(e / m);
+        slice_d<NS>(ldexp(X[i + (long long)j * ldx], -xexp[j]), xs + e, stride);
+    }
+}
+
+// ------------------------------------------------------------- products
+
+// Panel: W = F[rows]^T X[rows] for one (item, rhs tile), exact 128-bit sums.
+// F slices are column-major (ld n), X slices column-major (ld ldx); rows of
+// a stage are contiguous in both, so stages are staged with 16-byte
+// cp.async copies.  Block sizes and chunk offsets are multiples of 64.
+template <int NSA, int NSB, int DMAX>
+__global__ void __launch_bounds__(kSThreads) sp_panel_kernel(
+    const SPanelItem *__restrict__ items, const bf16 *__restrict__ apool, long long astride,
+    const bf16 *__restrict__ xs, long long xstride, int ldx, int nrhs, __int128 *__restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16 *As = reinterpret_cast<bf16 *>(smem);          // [NSA][ST][SLD]
+    bf16 *Bs = As + NSA * ST * SLD;                      // [NSB][ST][SLD]
+    const SPanelItem it = items[blockIdx.x];
+    const int j0 = blockIdx.y * ST;
+    const int nj = min(ST, nrhs - j0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int m0 = (warp >> 2) * 32, n0 = (warp & 3) * 16;
+    const int g = lane >> 2, t = lane & 3;
+    __int128 *P = partials + it.p * nrhs + (long long)it.chunk * it.rank * nrhs;
+
+    for (int kt = 0; kt < it.rank; kt += ST) {
+        const int nk = min(ST, it.rank - kt);
+        __int128 W[2][2][4];
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) W[fm][fn][i] = 0;
+        for (int s0 = 0; s0 < it.len; s0 += SK) {
+            __syncthreads();
+            // 8-element chunks: (slice, row-of-tile, chunk of 8 along the stage)
+            for (int e = tid; e < NSA * ST * (SK / 8); e += kSThreads) {
+                const int c = e % (SK / 8), m = (e / (SK / 8)) % ST, p = e / ((SK / 8) * ST);
+                const bool ok = m < nk;
+                const bf16 *src = apool + p * astride + it.f + (long long)(it.r0 + s0 + c * 8) +
+                                  (long long)(kt + (ok ? m : 0)) * it.n;
+                cp16(As + (p * ST + m) * SLD + c * 8, src, ok);
+            }
+            for (int e = tid; e < NSB * ST * (SK / 8); e += kSThreads) {
+                const int c = e % (SK / 8), n = (e / (SK / 8)) % ST, q = e / ((SK / 8) * ST);
+                const bool ok = n < nj;
+                const bf16 *src = xs + q * xstride + (long long)(it.in0 + it.r0 + s0 + c * 8) +
+                                  (long long)(j0 + (ok ? n : 0)) * ldx;
+                cp16(Bs + (q * ST + n) * SLD + c * 8, src, ok);
+            }
+            cp_wait_all();
+            __syncthreads();
+            stage_products<NSA, NSB, DMAX>(W, As, Bs, m0, n0, lane);
+        }
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int m = m0 + fm * 16 + g + (i >= 2 ? 8 : 0);
+                    const int n = n0 + fn * 8 + 2 * t + (i & 1);
+                    if (m < nk && n < nj) P[(kt + m) + (long long)(j0 + n) * it.rank] = W[fm][fn][i];
+                }
+    }
+}
+
+// Reduce: T = sig o 2^(E) sum_c W_c as double-double.
+template <int DMAX>
+__global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items,
+                                 const __int128 *__restrict__ partials, const int *__restrict__ aexp,
+                                 const int *__restrict__ xexp, const double *__restrict__ sigbase,
+                                 int nrhs, double *__restrict__ T, long long lo_off)
+{
+    const SReduceItem R = items[blockIdx.x];
+    const long long cnt = (long long)R.rank * nrhs;
+    const long long e = (long long)blockIdx.y * blockDim.x + threadIdx.x;
+    if (e >= cnt) return;
+    const int k = (int)(e % R.rank), j = (int)(e / R.rank);
+    __int128 W = 0;
+    for (int c = 0; c < R.nch; ++c) W += partials[R.p * nrhs + (long long)c * cnt + e];
+    double hi, lo;
+    i128_to_dd(W, hi, lo);
+    const int E = aexp[R.fexp + k] + xexp[j] - 7 * DMAX;
+    hi = ldexp(hi, E);
+    lo = ldexp(lo, E);
+    if (R.sig >= 0) {
+        const double s = sigbase[R.sig + k];
+        const double p = hi * s;
+        const double err = fma(hi, s, -p);
+        const double l2 = fma(lo, s, err);
+        two_sum(p, l2, hi, lo);
+    }
+    T[R.t * nrhs + e] = hi;
+    T[lo_off + R.t * nrhs + e] = lo;
+}
+
+// Slices of the double-double panel results, one exponent per (block,
+// column) over the block's rank rows; one warp per (block, column).  Rows
+// [rank, rp) of the slice panel are zero.
+template <int NS>
+__global__ void sp_tslice_kernel(const SReduceItem *__restrict__ items, int nitems,
+                                 const double *__restrict__ T, long long lo_off, int nrhs,
+                                 bf16 *__restrict__ ts, long long tstride, int *__restrict__ texp)
+{
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (long long)nitems * nrhs) return;
+    const int b = (int)(w / nrhs), j = (int)(w % nrhs);
+    const SReduceItem R = items[b];
+    const double *th = T + R.t * nrhs + (long long)j * R.rank;
+    const double *tl = lo_off >= 0 ? th + lo_off : nullptr;
+    double mx = 0.0;
+    for (int k = lane; k < R.rank; k += 32) mx = fmax(mx, fabs(th[k]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = scale_exp(mx);
+    if (lane == 0) texp[(long long)b * nrhs + j] = e;
+    bf16 *out = ts + R.tpad * nrhs + (long long)j * R.rp;
+    const bf16 zero = __float2bfloat16(0.0f);
+    for (int k = lane; k < R.rp; k += 32) {
+        if (k < R.rank) {
+            slice_dd<NS>(ldexp(th[k], -e), tl ? ldexp(tl[k], -e) : 0.0, out + k, tstride);
+        } else {
+#pragma unroll
+            for (int p = 0; p < NS; ++p) out[k + p * tstride] = zero;
+        }
+    }
+}
+
+// Expand: Y = alpha * sum_terms A_t B_t + beta * Bin over one 64-row tile.
+// A slices are row-major (row stride lda, zero padded to a multiple of 8),
+// B is either the T-slice panel of a block (ld ldb = padded rank) or the X
+// slices (leaf terms); everything is staged with 16-byte cp.async copies.
+template <int NSA, int NSB, int DMAX>
+__global__ void __launch_bounds__(kSThreads) sp_expand_kernel(
+    const STerm *__restrict__ terms, const int *__restrict__ tile_row0,
+    const int *__restrict__ tile_begin, const bf16 *__restrict__ apool, long long astride,
+    const int *__restrict__ aexp, const bf16 *__restrict__ ts, long long tstride,
+    const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int ldx,
+    const int *__restrict__ xexp, int nrhs, double alpha, const double *__restrict__ Bin,
+    int ldbin, double beta, double *__restrict__ Y, int ldy)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16 *As = reinterpret_cast<bf16 *>(smem);          // [NSA][ST][SLD]
+    bf16 *Bs = As + NSA * ST * SLD;                      // [NSB][ST][SLD]
+    __shared__ int rexp[ST], cexp[ST];
+    const int tile = blockIdx.x;
+    const int row0 = tile_row0[tile];
+    const int j0 = blockIdx.y * ST;
+    const int nj = min(ST, nrhs - j0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int m0 = (warp >> 2) * 32, n0 = (warp & 3) * 16;
+    const int g = lane >> 2, t = lane & 3;
+
+    double acch[2][2][4], accl[2][2][4];
+#pragma unroll
+    for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+        for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acch[fm][fn][i] = accl[fm][fn][i] = 0.0;
+
+    for (int q = tile_begin[tile]; q < tile_begin[tile + 1]; ++q) {
+        const STerm tt = terms[q];
+        __syncthreads();
+        if (tid < ST) {
+            rexp[tid] = aexp[tt.aexp + tid];
+            cexp[tid] = tid < nj ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + j0 + tid]
+                                               : xexp[j0 + tid])
+                                 : 0;
+        }
+        __int128 W[2][2][4];
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) W[fm][fn][i] = 0;
+        const int Kp = (tt.K + 7) & ~7;          // stored (zero padded) columns of A / rows of B
+        for (int k0 = 0; k0 < tt.K; k0 += SK) {
+            __syncthreads();
+            for (int e = tid; e < NSA * ST * (SK / 8); e += kSThreads) {
+                const int c = e % (SK / 8), m = (e / (SK / 8)) % ST, p = e / ((SK / 8) * ST);
+                const bool ok = k0 + c * 8 < Kp;
+                const bf16 *src = apool + p * astride + tt.a + (long long)m * tt.lda + (ok ? k0 + c * 8 : 0);
+                cp16(As + (p * ST + m) * SLD + c * 8, src, ok);
+            }
+            for (int e = tid; e < NSB * ST * (SK / 8); e += kSThreads) {
+                const int c = e % (SK / 8), n = (e / (SK / 8)) % ST, q2 = e / ((SK / 8) * ST);
+                const bool ok = n < nj && k0 + c * 8 < Kp;
+                const bf16 *src;
+                if (tt.src == 0)
+                    src = ts + q2 * tstride + tt.b * nrhs + (long long)(j0 + (ok ? n : 0)) * tt.ldb +
+                          (ok ? k0 + c * 8 : 0);
+                else
+                    src = xs + q2 * xstride + (long long)(tt.x_row0 + (ok ? k0 + c * 8 : 0)) +
+                          (long long)(j0 + (ok ? n : 0)) * ldx;
+                cp16(Bs + (q2 * ST + n) * SLD + c * 8, src, ok);
+            }
+            cp_wait_all();
+            __syncthreads();
+            stage_products<NSA, NSB, DMAX>(W, As, Bs, m0, n0, lane);
+        }
+        // term -> double-double, accumulated with error-free sums
+#pragma unroll
+        for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+            for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int m = m0 + fm * 16 + g + (i >= 2 ? 8 : 0);
+                    const int n = n0 + fn * 8 + 2 * t + (i & 1);
+                    double h, l;
+                    i128_to_dd(W[fm][fn][i], h, l);
+                    const int E = rexp[m] + cexp[n] - 7 * DMAX;
+                    h = ldexp(h, E);
+                    l = ldexp(l, E);
+                    double s2, e2;
+                    two_sum(acch[fm][fn][i], h, s2, e2);
+                    acch[fm][fn][i] = s2;
+                    accl[fm][fn][i] += e2 + l;
+                }
+    }
+#pragma unroll
+    for (int fm = 0; fm < 2; ++fm)
+#pragma unroll
+        for (int fn = 0; fn < 2; ++fn)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int m = m0 + fm * 16 + g + (i >= 2 ? 8 : 0);
+                const int n = n0 + fn * 8 + 2 * t + (i & 1);
+                if (n >= nj) continue;
+                const double ah = alpha * acch[fm][fn][i], al = alpha * accl[fm][fn][i];
+                double out;
+                if (beta == 0.0) {
+                    out = ah + al;
+                } else {
+                    const double b0 = beta * Bin[row0 + m + (long long)(j0 + n) * ldbin];
+                    double s2, e2;
+                    two_sum(b0, ah, s2, e2);
+                    out = s2 + (e2 + al);
+                }
+                Y[row0 + m + (long long)(j0 + n) * ldy] = out;
+            }
+}
+
+// ------------------------------------------------------------- host side
+
+constexpr int kNS = 8;      // slices of the FP64-accurate products
+constexpr int kD = 9;       // keep pairs p + q <= 9
+
+static long long al32(long long x) { return (x + 31) & ~31LL; }
+static int pad8(int x) { return (x + 7) & ~7; }
+
+template <class T>
+static int dev_vec(const std::vector<T> &v, T **dst, long long *bytes)
+{
+    DG_CUDA(cudaMalloc((void **)dst, std::max<size_t>(v.size(), 1) * sizeof(T)));
+    *bytes += (long long)(std::max<size_t>(v.size(), 1) * sizeof(T));
+    if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+static void free_sschedule(SSchedule &A)
+{
+    cudaFree(A.d_items);
+    cudaFree(A.d_reduces);
+    cudaFree(A.d_tile_row0);
+    cudaFree(A.d_tile_begin);
+    cudaFree(A.d_terms);
+    A.d_items = nullptr;
+    A.d_reduces = nullptr;
+    A.d_tile_row0 = A.d_tile_begin = nullptr;
+    A.d_terms = nullptr;
+}
+
+void sliced_free(Plan *p)
+{
+    Sliced *S = (Sliced *)p->sliced;
+    if (!S) return;
+    cudaFree(S->pool);
+    cudaFree(S->exps);
+    free_sschedule(S->apply);
+    cudaFree(S->xs);
+    cudaFree(S->xexp);
+    cudaFree(S->work);
+    delete S;
+    p->sliced = nullptr;
+}
+
+static size_t panel_smem(int nsa, int nsb) { return (size_t)(nsa + nsb) * ST * SLD * sizeof(bf16); }
+
+static int upload_sschedule(SSchedule &A, long long *bytes)
+{
+    int rc;
+    if ((rc = dev_vec(A.items, &A.d_items, bytes)) || (rc = dev_vec(A.reduces, &A.d_reduces, bytes)) ||
+        (rc = dev_vec(A.tile_row0, &A.d_tile_row0, bytes)) ||
+        (rc = dev_vec(A.tile_begin, &A.d_tile_begin, bytes)) || (rc = dev_vec(A.terms, &A.d_terms, bytes)))
+        return rc;
+    return 0;
+}
+
+int sliced_build(Plan *p, int ns, cudaStream_t st)
+{
+    sliced_free(p);
+    if (ns != kNS) return fail(DPLR_GPU_EINVAL, "sliced products: %d slices not built", ns);
+    for (const LeafDesc &L : p->leaves)
+        if (L.b % ST != 0 || L.row0 % ST != 0)
+            return fail(DPLR_GPU_EINVAL, "sliced products need leaf sizes that are multiples of %d", ST);
+    Sliced *S = new Sliced();
+    p->sliced = S;
+    S->ns = ns;
+
+    // layout: V column-major (ld n), U row-major (stride pad8(rank)), leaves row-major
+    std::vector<long long> vs_off(p->lr.size()), us_off(p->lr.size()), ds_off(p->leaves.size());
+    std::vector<int> ev_off(p->lr.size()), eu_off(p->lr.size()), ed_off(p->leaves.size());
+    std::vector<SliceJob> vj;
+    std::vector<RowSliceJob> uj;
+    std::vector<int> vbase, ubase;
+    long long el = 0;
+    int nexp = 0, ncols = 0, nrows = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        const int rp = pad8(L.rank);
+        vs_off[b] = el;
+        el += al32((long long)L.n * L.rank);
+        us_off[b] = el;
+        el += al32((long long)L.n * rp);
+        ev_off[b] = nexp;
+        nexp += L.rank;
+        eu_off[b] = nexp;
+        nexp += L.n;
+        if (L.rank == 0) continue;
+        vbase.push_back(ncols);
+        vj.push_back(SliceJob{L.v, vs_off[b], L.n, L.n, L.rank, ev_off[b]});
+        ncols += L.rank;
+        ubase.push_back(nrows);
+        uj.push_back(RowSliceJob{L.u, us_off[b], L.n, L.n, L.rank, rp, eu_off[b]});
+        nrows += L.n;
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        ds_off[i] = el;
+        el += al32((long long)L.b * L.b);
+        ed_off[i] = nexp;
+        nexp += L.b;
+        ubase.push_back(nrows);
+        uj.push_back(RowSliceJob{L.d, ds_off[i], L.b, L.b, L.b, L.b, ed_off[i]});
+        nrows += L.b;
+    }
+    S->stride = al32(std::max<long long>(el, 1));
+    cudaError_t e = cudaMalloc((void **)&S->pool, (size_t)ns * S->stride * sizeof(bf16));
+    if (e != cudaSuccess) return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate slices");
+    S->bytes += (long long)ns * S->stride * 2;
+    S->nexp = nexp;
+    int rc;
+    if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &S->exps, &S->bytes))) return rc;
+    {
+        SliceJob *d_vj = nullptr;
+        RowSliceJob *d_uj = nullptr;
+        int *d_vb = nullptr, *d_ub = nullptr;
+        long long tmp = 0;
+        if ((rc = dev_vec(vj, &d_vj, &tmp)) || (rc = dev_vec(vbase, &d_vb, &tmp)) ||
+            (rc = dev_vec(uj, &d_uj, &tmp)) || (rc = dev_vec(ubase, &d_ub, &tmp)))
+            return rc;
+        if (ncols > 0) {
+            slice_cols_kernel<kNS><<<ncols, 256, 0, st>>>(d_vj, d_vb, (int)vj.size(), p->pool, S->pool,
+                                                          S->stride, S->exps);
+            note_launch();
+        }
+        if (nrows > 0) {
+            slice_rows_kernel<kNS><<<(nrows + 127) / 128, 128, 0, st>>>(
+                d_uj, d_ub, (int)uj.size(), nrows, p->pool, S->pool, S->stride, S->exps);
+            note_launch();
+        }
+        cudaError_t e2 = cudaGetLastError();
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+        cudaFree(d_vj);
+        cudaFree(d_uj);
+        cudaFree(d_vb);
+        cudaFree(d_ub);
+        if (e2 != cudaSuccess) return fail(DPLR_GPU_ECUDA, "slicing: %s", cudaGetErrorString(e2));
+    }
+
+    // op-N schedule
+    SSchedule &A = S->apply;
+    const int CH = 1024;
+    long long poff = 0, tpad = 0;
+    std::vector<int> ridx(p->lr.size(), -1);
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        int nch = (L.n + CH - 1) / CH;
+        for (int c = 0; c < nch; ++c) {
+            SPanelItem it;
+            it.f = vs_off[b];
+            it.p = poff;
+            it.n = L.n;
+            it.rank = L.rank;
+            it.in0 = L.col0;
+            it.r0 = c * CH;
+            it.len = std::min(CH, L.n - c * CH);
+            it.chunk = c;
+            A.items.push_back(it);
+        }
+        ridx[b] = (int)A.reduces.size();
+        A.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], pad8(L.rank), tpad});
+        poff += (long long)nch * L.rank;
+        tpad += pad8(L.rank);
+        A.max_rank = std::max(A.max_rank, L.rank);
+    }
+    A.partial_per_rhs = poff;
+    A.t_per_rhs = p->total_rank;
+    A.tpad_per_rhs = tpad;
+    const int ntiles = p->m / ST;
+    std::vector<std::vector<STerm>> per(ntiles);
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        const int rp = pad8(L.rank);
+        for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += ST) {
+            STerm tt;
+            tt.a = us_off[b] + (long long)(t0 - L.row0) * rp;
+            tt.b = A.reduces[ridx[b]].tpad;
+            tt.lda = rp;
+            tt.K = L.rank;
+            tt.aexp = eu_off[b] + (t0 - L.row0);
+            tt.src = 0;
+            tt.ldb = rp;
+            tt.x_row0 = 0;
+            tt.blk = ridx[b];
+            per[t0 / ST].push_back(tt);
+        }
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += ST) {
+            STerm tt;
+            tt.a = ds_off[i] + (long long)(t0 - L.row0) * L.b;
+            tt.b = 0;
+            tt.lda = L.b;
+            tt.K = L.b;
+            tt.aexp = ed_off[i] + (t0 - L.row0);
+            tt.src = 1;
+            tt.ldb = 0;
+            tt.x_row0 = L.row0;
+            tt.blk = -1;
+            per[t0 / ST].push_back(tt);
+        }
+    }
+    for (int t = 0; t < ntiles; ++t) {
+        A.tile_row0.push_back(t * ST);
+        A.tile_begin.push_back((int)A.terms.size());
+        A.terms.insert(A.terms.end(), per[t].begin(), per[t].end());
+    }
+    A.tile_begin.push_back((int)A.terms.size());
+    if ((rc = upload_sschedule(A, &S->bytes))) return rc;
+    DG_CUDA(cudaFuncSetAttribute(sp_panel_kernel<kNS, kNS, kD>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
+    DG_CUDA(cudaFuncSetAttribute(sp_expand_kernel<kNS, kNS, kD>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
+    return 0;
+}
+
+// Scratch of one sliced apply with nrhs columns: X slices, exponents,
+// 128-bit partials, DD T, T slices and their exponents.
+struct SWork {
+    __int128 *partials;
+    double *T;
+    long long lo_off;
+    bf16 *ts;
+    long long tstride;
+    int *texp;
+};
+
+static int sliced_scratch(Sliced *S, const SSchedule &A, int m, int nrhs, int ns, SWork &w)
+{
+    const size_t xs_need = (size_t)ns * m * nrhs;
+    if (S->xs_elems < xs_need) {
+        cudaFree(S->xs);
+        S->xs = nullptr;
+        S->xs_elems = 0;
+        if (cudaMalloc((void **)&S->xs, xs_need * sizeof(bf16)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate X slices");
+        S->xs_elems = xs_need;
+    }
+    if (S->xexp_n < (size_t)nrhs) {
+        cudaFree(S->xexp);
+        S->xexp = nullptr;
+        if (cudaMalloc((void **)&S->xexp, nrhs * sizeof(int)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
+        S->xexp_n = nrhs;
+    }
+    const size_t part_bytes = (size_t)A.partial_per_rhs * nrhs * sizeof(__int128);
+    const size_t t_bytes = (size_t)2 * A.t_per_rhs * nrhs * sizeof(double);
+    const size_t ts_elems = (size_t)A.tpad_per_rhs * nrhs;
+    const size_t ts_bytes = ((size_t)ns * ts_elems * sizeof(bf16) + 255) & ~(size_t)255;
+    const size_t te_bytes = (size_t)A.reduces.size() * nrhs * sizeof(int);
+    const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes + 1024;
+    if (S->work_bytes < need) {
+        cudaFree(S->work);
+        S->work = nullptr;
+        S->work_bytes = 0;
+        if (cudaMalloc(&S->work, need) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate scratch");
+        S->work_bytes = need;
+    }
+    char *base = reinterpret_cast<char *>(S->work);
+    w.partials = reinterpret_cast<__int128 *>(base);
+    w.T = reinterpret_cast<double *>(base + part_bytes);
+    w.lo_off = A.t_per_rhs * nrhs;
+    w.ts = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes);
+    w.tstride = (long long)ts_elems;
+    w.texp = reinterpret_cast<int *>(base + part_bytes + t_bytes + ts_bytes);
+    return 0;
+}
+
+int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B, int ldb,
+                    double *R, int ldr, cudaStream_t st)
+{
+    Sliced *S = (Sliced *)p->sliced;
+    if (!S) return fail(DPLR_GPU_ESTATE, "sliced residual: plan has no sliced factors");
+    if (nrhs <= 0 || p->m == 0) return 0;
+    const int m = p->m;
+    const SSchedule &A = S->apply;
+    SWork w;
+    int rc = sliced_scratch(S, A, m, nrhs, kNS, w);
+    if (rc) return rc;
+    const long long xstride = (long long)m * nrhs;
+    {
+        ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * kNS * m * nrhs);
+        xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, S->xexp);
+        note_launch();
+        long long cnt = (long long)m * nrhs;
+        int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
+        xslice_kernel<kNS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, S->xexp, S->xs, xstride);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    const unsigned rtiles = (unsigned)((nrhs + ST - 1) / ST);
+    const size_t smem = panel_smem(kNS, kNS);
+    int npairs = 0;
+    for (int d = 2; d <= kD; ++d)
+        for (int pp = std::max(1, d - kNS); pp <= std::min(kNS, d - 1); ++pp) ++npairs;
+    if (!A.items.empty()) {
+        double fl = 0, by = 0;
+        for (const SPanelItem &it : A.items) {
+            fl += 2.0 * it.len * it.rank * nrhs;
+            by += 2.0 * kNS * ((double)it.len * it.rank + (double)it.len * nrhs) + 16.0 * it.rank * nrhs;
+        }
+        {
+            ProfScope ps("sliced_panel", st, fl * npairs, by);
+            sp_panel_kernel<kNS, kNS, kD><<<dim3((unsigned)A.items.size(), rtiles), kSThreads, smem, st>>>(
+                A.d_items, S->pool, S->stride, S->xs, xstride, m, nrhs, w.partials);
+            note_launch();
+            DG_CUDA(cudaGetLastError());
+        }
+        ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
+        long long maxcnt = (long long)A.max_rank * nrhs;
+        sp_reduce_kernel<kD><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+            A.d_reduces, w.partials, S->exps, S->xexp, p->pool, nrhs, w.T, w.lo_off);
+        note_launch();
+        long long warps = (long long)A.reduces.size() * nrhs;
+        sp_tslice_kernel<kNS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            A.d_reduces, (int)A.reduces.size(), w.T, w.lo_off, nrhs, w.ts, w.tstride, w.texp);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    const unsigned ntiles = (unsigned)A.tile_row0.size();
+    if (ntiles) {
+        double fl = 0, by = 0;
+        for (const STerm &t : A.terms) {
+            fl += 2.0 * ST * t.K * nrhs;
+            by += 2.0 * kNS * ((double)ST * t.K) + 2.0 * kNS * t.K * nrhs;
+        }
+        ProfScope ps("sliced_expand", st, fl * npairs, by + 16.0 * m * nrhs);
+        sp_expand_kernel<kNS, kNS, kD><<<dim3(ntiles, rtiles), kSThreads, smem, st>>>(
+            A.d_terms, A.d_tile_row0, A.d_tile_begin, S->pool, S->stride, S->exps, w.ts, w.tstride,
+            w.texp, S->xs, xstride, m, S->xexp, nrhs, -1.0, B, ldb, 1.0, R, ldr);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    return 0;
+}
+
+
+// ====================================================== low-precision solve
+
+// Slice counts of the inner solve: kMSMin..kMSMax slices, pairs p + q <= NS + 1.
+constexpr int kMSMin = 3, kMSMax = 6;
+
+static int pair_count(int ns, int dmax)
+{
+    int n = 0;
+    for (int d = 2; d <= dmax; ++d)
+        for (int p = std::max(1, d - ns); p <= std::min(ns, d - 1); ++p) ++n;
+    return n;
+}
+
+void mixed_free(Plan *p)
+{
+    MixedSliced *M = (MixedSliced *)p->mixed;
+    if (!M) return;
+    cudaFree(M->pool);
+    cudaFree(M->exps);
+    for (SSchedule &L : M->level) free_sschedule(L);
+    free_sschedule(M->leaf);
+    cudaFree(M->xs);
+    cudaFree(M->xexp);
+    cudaFree(M->work);
+    delete M;
+    p->mixed = nullptr;
+}
+
+template <int NS>
+static int mixed_slice_t(const std::vector<SliceJob> &vj, const std::vector<int> &vbase, int ncols,
+                         const std::vector<RowSliceJob> &zj, const std::vector<RowSliceJob> &lj,
+                         const double *vpool, const double *zpool, const double *lpool, MixedSliced *M,
+                         cudaStream_t st)
+{
+    SliceJob *d_vj = nullptr;
+    RowSliceJob *d_zj = nullptr, *d_lj = nullptr;
+    int *d_vb = nullptr, *d_zb = nullptr, *d_lb = nullptr;
+    std::vector<int> zb, lb;
+    int zr = 0, lr = 0;
+    for (auto &j : zj) { zb.push_back(zr); zr += j.rows; }
+    for (auto &j : lj) { lb.push_back(lr); lr += j.rows; }
+    long long tmp = 0;
+    int rc = 0;
+    if ((rc = dev_vec(vj, &d_vj, &tmp)) || (rc = dev_vec(vbase, &d_vb, &tmp)) ||
+        (rc = dev_vec(zj, &d_zj, &tmp)) || (rc = dev_vec(zb, &d_zb, &tmp)) ||
+        (rc = dev_vec(lj, &d_lj, &tmp)) || (rc = dev_vec(lb, &d_lb, &tmp)))
+        goto out;
+    if (ncols > 0) {
+        slice_cols_kernel<NS><<<ncols, 256, 0, st>>>(d_vj, d_vb, (int)vj.size(), vpool, M->pool, M->stride,
+                                                     M->exps);
+        note_launch();
+    }
+    // Z_l live in the factorisation's pool, leaf inverses in its leaf pool
+    if (zr > 0) {
+        slice_rows_kernel<NS><<<(zr + 127) / 128, 128, 0, st>>>(d_zj, d_zb, (int)zj.size(), zr, zpool, M->pool,
+                                                               M->stride, M->exps);
+        note_launch();
+    }
+    if (lr > 0) {
+        slice_rows_kernel<NS><<<(lr + 127) / 128, 128, 0, st>>>(d_lj, d_lb, (int)lj.size(), lr, lpool, M->pool,
+                                                               M->stride, M->exps);
+        note_launch();
+    }
+    {
+        cudaError_t e2 = cudaGetLastError();
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+        if (e2 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "mixed slicing: %s", cudaGetErrorString(e2));
+    }
+    if (!rc) {
+        cudaError_t e3 = cudaFuncSetAttribute(sp_panel_kernel<NS, NS, NS + 1>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)panel_smem(NS, NS));
+        if (e3 == cudaSuccess)
+            e3 = cudaFuncSetAttribute(sp_expand_kernel<NS, NS, NS + 1>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(NS, NS));
+        if (e3 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "mixed solve: %s", cudaGetErrorString(e3));
+    }
+out:
+    cudaFree(d_vj);
+    cudaFree(d_vb);
+    cudaFree(d_zj);
+    cudaFree(d_zb);
+    cudaFree(d_lj);
+    cudaFree(d_lb);
+    return rc;
+}
+
+int mixed_build(Plan *p, int ns, cudaStream_t st)
+{
+    mixed_free(p);
+    Fact *F = (Fact *)p->fact;
+    if (!F) return fail(DPLR_GPU_ESTATE, "mixed solve: plan is not factored");
+    if (ns < kMSMin || ns > kMSMax)
+        return fail(DPLR_GPU_EINVAL, "mixed solve: %d slices (supported: %d to %d)", ns, kMSMin, kMSMax);
+    for (const LeafDesc &L : p->leaves)
+        if (L.b % ST != 0 || L.row0 % ST != 0)
+            return fail(DPLR_GPU_EINVAL, "sliced products need leaf sizes that are multiples of %d", ST);
+    MixedSliced *M = new MixedSliced();
+    p->mixed = M;
+    M->ns = ns;
+    const int m = p->m;
+    const int nlev = (int)F->lv.size();
+
+    // slice layout: V (column-major), Z_l (row-major, stride pad8(width)), leaf inverses (row-major)
+    std::vector<long long> vs_off(p->lr.size()), zs_off(nlev), ls_off(p->leaves.size());
+    std::vector<int> ev_off(p->lr.size()), ez_off(nlev), el_off(p->leaves.size());
+    std::vector<SliceJob> vj;
+    std::vector<RowSliceJob> zj, lj;
+    std::vector<int> vbase;
+    long long el = 0;
+    int nexp = 0, ncols = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        vs_off[b] = el;
+        el += al32((long long)L.n * L.rank);
+        ev_off[b] = nexp;
+        nexp += L.rank;
+        if (L.rank == 0) continue;
+        vbase.push_back(ncols);
+        vj.push_back(SliceJob{L.v, vs_off[b], L.n, L.n, L.rank, ev_off[b]});
+        ncols += L.rank;
+    }
+    for (int l = 0; l < nlev; ++l) {
+        const int w = F->lv[l].width, wp = pad8(w);
+        zs_off[l] = el;
+        el += al32((long long)m * wp);
+        ez_off[l] = nexp;
+        nexp += m;
+        if (w == 0) continue;
+        zj.push_back(RowSliceJob{F->zoff[l], zs_off[l], m, m, w, wp, ez_off[l]});
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        ls_off[i] = el;
+        el += al32((long long)L.b * L.b);
+        el_off[i] = nexp;
+        nexp += L.b;
+        lj.push_back(RowSliceJob{F->leafoff[i], ls_off[i], L.b, L.b, L.b, L.b, el_off[i]});
+    }
+    M->stride = al32(std::max<long long>(el, 1));
+    if (cudaMalloc((void **)&M->pool, (size_t)ns * M->stride * sizeof(bf16)) != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
+    M->bytes += (long long)ns * M->stride * 2;
+    int rc;
+    if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &M->exps, &M->bytes))) return rc;
+    switch (ns) {
+    case 3: rc = mixed_slice_t<3>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    case 4: rc = mixed_slice_t<4>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    case 5: rc = mixed_slice_t<5>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    default: rc = mixed_slice_t<6>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    }
+    if (rc) return rc;
+
+    // schedules: global reduce numbering over blocks (T / W slice panels)
+    const int CH = 1024;
+    std::vector<long long> tpad(p->lr.size(), 0);
+    long long tp = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        tpad[b] = tp;
+        tp += pad8(p->lr[b].rank);
+    }
+    M->tpad_per_rhs = tp;
+    M->t_per_rhs = p->total_rank;
+    M->nblocks = (int)p->lr.size();
+    M->level.resize(nlev);
+    for (int l = 0; l < nlev; ++l) {
+        SSchedule &S = M->level[l];
+        long long poff = 0;
+        const int wp = pad8(F->lv[l].width);
+        for (int b : F->lv[l].blocks) {
+            const LRDesc &L = p->lr[b];
+            if (L.rank == 0) continue;
+            const int nch = (L.n + CH - 1) / CH;
+            for (int c = 0; c < nch; ++c) {
+                SPanelItem it;
+                it.f = vs_off[b];
+                it.p = poff;
+                it.n = L.n;
+                it.rank = L.rank;
+                it.in0 = L.col0;
+                it.r0 = c * CH;
+                it.len = std::min(CH, L.n - c * CH);
+                it.chunk = c;
+                S.items.push_back(it);
+            }
+            const int ridx = (int)S.reduces.size();
+            S.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], pad8(L.rank), tpad[b]});
+            poff += (long long)nch * L.rank;
+            S.max_rank = std::max(S.max_rank, L.rank);
+            for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += ST) {
+                STerm tt;
+                tt.a = zs_off[l] + (long long)t0 * wp;
+                tt.b = tpad[b];
+                tt.lda = wp;
+                tt.K = L.rank;
+                tt.aexp = ez_off[l] + t0;
+                tt.src = 0;
+                tt.ldb = pad8(L.rank);
+                tt.x_row0 = 0;
+                tt.blk = ridx;
+                S.tile_row0.push_back(t0);
+                S.tile_begin.push_back((int)S.terms.size());
+                S.terms.push_back(tt);
+            }
+        }
+        S.tile_begin.push_back((int)S.terms.size());
+        S.partial_per_rhs = poff;
+        S.t_per_rhs = p->total_rank;
+        S.tpad_per_rhs = tp;
+        if ((rc = upload_sschedule(S, &M->bytes))) return rc;
+    }
+    SSchedule &LS = M->leaf;
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += ST) {
+            STerm tt;
+            tt.a = ls_off[i] + (long long)(t0 - L.row0) * L.b;
+            tt.b = 0;
+            tt.lda = L.b;
+            tt.K = L.b;
+            tt.aexp = el_off[i] + (t0 - L.row0);
+            tt.src = 1;
+            tt.ldb = 0;
+            tt.x_row0 = L.row0;
+            tt.blk = -1;
+            LS.tile_row0.push_back(t0);
+            LS.tile_begin.push_back((int)LS.terms.size());
+            LS.terms.push_back(tt);
+        }
+    }
+    LS.tile_begin.push_back((int)LS.terms.size());
+    return upload_sschedule(LS, &M->bytes);
+}
+
+// Slice the columns of an m x n FP64 block (global exponent per column).
+template <int NS>
+static int slice_block(const double *X, int m, int ldx, int nrhs, bf16 *xs, int *xexp, cudaStream_t st)
+{
+    xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, xexp);
+    note_launch();
+    long long cnt = (long long)m * nrhs;
+    int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
+    xslice_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xexp, xs, (long long)m * nrhs);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Scratch of the inner solve, carved from one allocation.
+struct MWork {
+    __int128 *partials;
+    double *T, *W;
+    long long lo_off;
+    bf16 *ws;
+    long long wstride;
+    int *wexp;
+};
+
+static int mixed_scratch(MixedSliced *M, int m, int nrhs, MWork &w)
+{
+    const size_t xs_need = (size_t)M->ns * m * nrhs;
+    if (M->xs_elems < xs_need) {
+        cudaFree(M->xs);
+        M->xs = nullptr;
+        M->xs_elems = 0;
+        if (cudaMalloc((void **)&M->xs, xs_need * sizeof(bf16)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
+        M->xs_elems = xs_need;
+    }
+    if (M->xexp_n < (size_t)nrhs) {
+        cudaFree(M->xexp);
+        M->xexp = nullptr;
+        if (cudaMalloc((void **)&M->xexp, nrhs * sizeof(int)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate exponents");
+        M->xexp_n = nrhs;
+    }
+    long long part = 0;
+    for (const SSchedule &L : M->level) part = std::max(part, L.partial_per_rhs);
+    const size_t part_bytes = (size_t)part * nrhs * sizeof(__int128);
+    const size_t t_bytes = (size_t)2 * M->t_per_rhs * nrhs * sizeof(double);
+    const size_t w_bytes = (size_t)M->t_per_rhs * nrhs * sizeof(double);
+    const size_t ws_bytes = ((size_t)M->ns * M->tpad_per_rhs * nrhs * sizeof(bf16) + 255) & ~(size_t)255;
+    size_t maxred = 0;
+    for (const SSchedule &L : M->level) maxred = std::max(maxred, L.reduces.size());
+    const size_t we_bytes = std::max<size_t>(maxred, 1) * nrhs * sizeof(int);
+    const size_t need = part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes + 1024;
+    if (M->work_bytes < need) {
+        cudaFree(M->work);
+        M->work = nullptr;
+        M->work_bytes = 0;
+        if (cudaMalloc(&M->work, need) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate scratch");
+        M->work_bytes = need;
+    }
+    char *base = reinterpret_cast<char *>(M->work);
+    w.partials = reinterpret_cast<__int128 *>(base);
+    w.T = reinterpret_cast<double *>(base + part_bytes);
+    w.lo_off = M->t_per_rhs * nrhs;
+    w.W = reinterpret_cast<double *>(base + part_bytes + t_bytes);
+    w.ws = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes + w_bytes);
+    w.wstride = M->tpad_per_rhs * nrhs;
+    w.wexp = reinterpret_cast<int *>(base + part_bytes + t_bytes + w_bytes + ws_bytes);
+    return 0;
+}
+
+template <int NS>
+static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const double *B, int ldb, double *X,
+                         int ldx, cudaStream_t st)
+{
+    constexpr int D = NS + 1;
+    const int m = p->m;
+    MWork w;
+    int rc = mixed_scratch(M, m, nrhs, w);
+    if (rc) return rc;
+    const long long xstride = (long long)m * nrhs;
+    const unsigned rtiles = (unsigned)((nrhs + ST - 1) / ST);
+    const size_t smem = panel_smem(NS, NS);
+    const double npairs = pair_count(NS, D);
+
+    // leaf step: X = Leaf^-1 B
+    if ((rc = slice_block<NS>(B, m, ldb, nrhs, M->xs, M->xexp, st))) return rc;
+    {
+        const SSchedule &LS = M->leaf;
+        double fl = 0;
+        for (const STerm &t : LS.terms) fl += 2.0 * ST * t.K * nrhs;
+        ProfScope ps("mixed_expand", st, fl * npairs, 0.0);
+        sp_expand_kernel<NS, NS, D><<<dim3((unsigned)LS.tile_row0.size(), rtiles), kSThreads, smem, st>>>(
+            LS.d_terms, LS.d_tile_row0, LS.d_tile_begin, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp,
+            M->xs, xstride, m, M->xexp, nrhs, 1.0, nullptr, 0, 0.0, X, ldx);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    for (int l = (int)M->level.size() - 1; l >= 0; --l) {
+        const SSchedule &S = M->level[l];
+        if (S.items.empty()) continue;
+        if ((rc = slice_block<NS>(X, m, ldx, nrhs, M->xs, M->xexp, st))) return rc;
+        double fl = 0;
+        for (const SPanelItem &it : S.items) fl += 2.0 * it.len * it.rank * nrhs;
+        {
+            ProfScope ps("mixed_panel", st, fl * npairs, 0.0);
+            sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rtiles), kSThreads, smem, st>>>(
+                S.d_items, M->pool, M->stride, M->xs, xstride, m, nrhs, w.partials);
+            note_launch();
+        }
+        long long maxcnt = (long long)S.max_rank * nrhs;
+        sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+            S.d_reduces, w.partials, M->exps, M->xexp, p->pool, nrhs, w.T, w.lo_off);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+        // capacitance in FP64 on the high parts
+        if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, w.T, w.W, nrhs, st))) return rc;
+        long long warps = (long long)S.reduces.size() * nrhs;
+        sp_tslice_kernel<NS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            S.d_reduces, (int)S.reduces.size(), w.W, -1, nrhs, w.ws, w.wstride, w.wexp);
+        note_launch();
+        double fu = 0;
+        for (const STerm &t : S.terms) fu += 2.0 * ST * t.K * nrhs;
+        ProfScope ps2("mixed_expand", st, fu * npairs, 0.0);
+        sp_expand_kernel<NS, NS, D><<<dim3((unsigned)S.tile_row0.size(), rtiles), kSThreads, smem, st>>>(
+            S.d_terms, S.d_tile_row0, S.d_tile_begin, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp,
+            M->xs, xstride, m, M->xexp, nrhs, -1.0, X, ldx, 1.0, X, ldx);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    return 0;
+}
+
+int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx, cudaStream_t st)
+{
+    MixedSliced *M = (MixedSliced *)p->mixed;
+    Fact *F = (Fact *)p->fact;
+    if (!M || !F) return fail(DPLR_GPU_ESTATE, "mixed solve: not prepared");
+    if (nrhs <= 0 || p->m == 0) return 0;
+    switch (M->ns) {
+    case 3: return mixed_solve_t<3>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    case 4: return mixed_solve_t<4>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    case 5: return mixed_solve_t<5>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    default: return mixed_solve_t<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    }
+}
+
+}  // namespace dg

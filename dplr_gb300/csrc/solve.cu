@@ -8,7 +8,7 @@
 //   dplr_gpu_solve_refined X with ||B - A X|| / ||B|| <= tol per column,
 //                          by iterative refinement whose residual is the
 //                          FP64 PLR apply of the original matrix.
-#include "internal.cuh"
+#include "sliced.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -97,8 +97,38 @@ int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int l
     return factor_solve(p, tr, n, B, ldb, X, ldx, (cudaStream_t)stream);
 }
 
+int dplr_gpu_prepare_sliced(dplr_gpu_plan plan, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_sliced: null plan");
+    return sliced_build(p, 8, (cudaStream_t)stream);
+}
+
+int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_mixed: null plan");
+    return mixed_build(p, slices, (cudaStream_t)stream);
+}
+
+int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *B, int ldb,
+                      double *R, int ldr, int flags, void *stream)
+{
+    Plan *p = (Plan *)plan;
+    if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_residual: null plan");
+    const int mm = std::max(p->m, 1);
+    if (n < 0 || ldx < mm || ldb < mm || ldr < mm)
+        return fail(DPLR_GPU_EINVAL, "dplr_gpu_residual: invalid n or leading dimension");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (flags & DPLR_GPU_RESIDUAL_SLICED) return sliced_residual(p, n, X, ldx, B, ldb, R, ldr, st);
+    int rc = axpby_device(p->m, n, 1.0, B, ldb, 0.0, R, ldr, st);
+    if (rc) return rc;
+    return apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, ldr, st, false);
+}
+
 int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, double *X, int ldx,
-                           double tol, int maxiter, double *rel_resid, int *iters, void *stream)
+                           double tol, int maxiter, int flags, double *rel_resid, int *iters,
+                           void *stream)
 {
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: null plan");
@@ -119,22 +149,33 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
     double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
     double *bn = D + (size_t)m * n, *rn = bn + n;
     std::vector<double> hb(n), hr(n);
+    const bool mixed = (flags & DPLR_GPU_SOLVE_MIXED) != 0;
+    if (mixed && !p->mixed) return fail(DPLR_GPU_ESTATE, "solve: mixed solve not prepared");
+    if ((flags & DPLR_GPU_RESIDUAL_SLICED) && !p->sliced)
+        return fail(DPLR_GPU_ESTATE, "solve: sliced residual not prepared");
+    auto inner = [&](const double *rhs, int ld, double *out, int ldo) -> int {
+        return mixed ? mixed_solve(p, n, rhs, ld, out, ldo, st) : factor_solve(p, 0, n, rhs, ld, out, ldo, st);
+    };
     if ((rc = colnorms_device(B, m, n, ldb, bn, st))) return rc;
     DG_CUDA(cudaMemcpyAsync(hb.data(), bn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if ((rc = factor_solve(p, 0, n, B, ldb, X, ldx, st))) return rc;
+    if ((rc = inner(B, ldb, X, ldx))) return rc;
     double worst = INFINITY;
     int it = 0;
     for (;;) {
-        // R = B - A X (FP64 apply of the original matrix)
-        if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
-        if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        // R = B - A X with the original matrix (FP64 apply, or exact-slice products)
+        if (flags & DPLR_GPU_RESIDUAL_SLICED) {
+            if ((rc = sliced_residual(p, n, X, ldx, B, ldb, R, m, st))) return rc;
+        } else {
+            if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
+            if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        }
         if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
         DG_CUDA(cudaMemcpyAsync(hr.data(), rn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         DG_CUDA(cudaStreamSynchronize(st));
         worst = 0.0;
         for (int j = 0; j < n; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
         if (worst <= tol || it >= maxiter) break;
-        if ((rc = factor_solve(p, 0, n, R, m, D, m, st))) return rc;
+        if ((rc = inner(R, m, D, m))) return rc;
         if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
         ++it;
     }
@@ -147,15 +188,15 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
 }
 
 int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb, double *X,
-                                int ldx, double tol, int maxiter, double *rel_resid, int *iters,
-                                void *stream)
+                                int ldx, double tol, int maxiter, int flags, double *rel_resid,
+                                int *iters, void *stream)
 {
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: null plan");
     if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1))
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: invalid arguments");
     if (n == 0 || p->m == 0) return dplr_gpu_solve_refined(plan, n, nullptr, 1, nullptr, 1, tol,
-                                                          maxiter, rel_resid, iters, stream);
+                                                          maxiter, flags, rel_resid, iters, stream);
     cudaStream_t st = (cudaStream_t)stream;
     const size_t cnt = (size_t)p->m * n;
     int rc = ensure_buffer(&p->xbuf, &p->xbuf_doubles, 2 * cnt);
@@ -163,7 +204,8 @@ int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int 
     double *dB = p->xbuf, *dX = p->xbuf + cnt;
     DG_CUDA(cudaMemcpy2DAsync(dB, sizeof(double) * p->m, B, sizeof(double) * ldb,
                               sizeof(double) * p->m, n, cudaMemcpyHostToDevice, st));
-    rc = dplr_gpu_solve_refined(plan, n, dB, p->m, dX, p->m, tol, maxiter, rel_resid, iters, stream);
+    rc = dplr_gpu_solve_refined(plan, n, dB, p->m, dX, p->m, tol, maxiter, flags, rel_resid, iters,
+                                stream);
     if (rc && rc != DPLR_GPU_ENOTCONV) return rc;
     DG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, dX, sizeof(double) * p->m,
                               sizeof(double) * p->m, n, cudaMemcpyDeviceToHost, st));

@@ -49,6 +49,36 @@ class GpuPlan:
                                ctypes.byref(mr))
         self.nnz, self.levels, self.max_rank = nnz.value, lev.value, mr.value
         self.factored = False
+        self.sliced = False
+        self.mixed = False
+
+    RESIDUAL_SLICED = 1
+    SOLVE_MIXED = 2
+
+    def prepare_mixed(self, slices: int = 6, stream=None) -> None:
+        """Sliced factor copies (3 to 6 bf16 slices) for the low-precision inner solve."""
+        _native.check(_native.lib().dplr_gpu_prepare_mixed(self._h, int(slices), _stream_ptr(stream)),
+                      "dplr_gpu_prepare_mixed")
+        self.mixed = True
+        self.mixed_slices = int(slices)
+
+    def prepare_sliced(self, stream=None) -> None:
+        """Exact-slice factor copies for the precise (tensor-core) residual."""
+        _native.check(_native.lib().dplr_gpu_prepare_sliced(self._h, _stream_ptr(stream)),
+                      "dplr_gpu_prepare_sliced")
+        self.sliced = True
+
+    def residual(self, x: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None,
+                 precise: bool = True, stream=None) -> torch.Tensor:
+        """out := b - A x (exact-slice products when precise)."""
+        _check_block(x, self.m, "x")
+        _check_block(b, self.m, "b")
+        out = torch.empty_like(b) if out is None else out
+        _check_block(out, self.m, "out")
+        _native.check(_native.lib().dplr_gpu_residual(
+            self._h, x.shape[0], x.data_ptr(), self.m, b.data_ptr(), self.m, out.data_ptr(),
+            self.m, self.RESIDUAL_SLICED if precise else 0, _stream_ptr(stream)), "dplr_gpu_residual")
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -102,15 +132,22 @@ class GpuPlan:
         return out
 
     def solve_refined(self, b: torch.Tensor, tol: float = 1e-12, maxiter: int = 10,
-                      out: torch.Tensor | None = None, stream=None, strict: bool = True):
-        """Refined FP64 solve; returns (x, relative residual, corrections).
-        With strict=False a solve that stops above `tol` is returned too."""
+                      out: torch.Tensor | None = None, stream=None, strict: bool = True,
+                      precise: bool | None = None, mixed: bool = False):
+        """Refined solve; returns (x, relative residual, corrections).  The
+        residual uses exact-slice products when `precise` (default: when
+        the plan has them).  With strict=False a solve that stops above
+        `tol` is returned too."""
+        if precise is None:
+            precise = self.sliced
         _check_block(b, self.m, "b")
         out = torch.empty_like(b) if out is None else out
         _check_block(out, self.m, "out")
         res, its = ctypes.c_double(), ctypes.c_int()
         rc = _native.lib().dplr_gpu_solve_refined(self._h, b.shape[0], b.data_ptr(), self.m,
                                                   out.data_ptr(), self.m, tol, maxiter,
+                                                  (self.RESIDUAL_SLICED if precise else 0)
+                                                  | (self.SOLVE_MIXED if mixed else 0),
                                                   ctypes.byref(res), ctypes.byref(its),
                                                   _stream_ptr(stream))
         if rc != -5 or strict:

@@ -71,13 +71,46 @@ DPLR_API long long dplr_gpu_factor_device_bytes(dplr_gpu_plan plan);
 DPLR_API int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int ldb,
                             double *X, int ldx, void *stream);
 
-/* X := A^-1 B refined until max_j ||B_j - A X_j|| / ||B_j|| <= tol, the
- * residual computed by the FP64 apply of A; at most maxiter corrections.
- * Reports the final relative residual and the number of corrections;
- * returns DPLR_GPU_ENOTCONV if the tolerance was not reached. */
+/* Exact-slice copies of the factors for the precise residual: every
+ * factor cut into 8 bf16 slices of 7 bits with a power-of-two scale per row
+ * or column, so that products run on the tensor cores with exact integer
+ * accumulation.  Needs leaf sizes that are multiples of 64. */
+DPLR_API int dplr_gpu_prepare_sliced(dplr_gpu_plan plan, void *stream);
+
+/* R := B - A X (device arrays).  flags: DPLR_GPU_RESIDUAL_SLICED computes
+ * the products from the exact slices (needs dplr_gpu_prepare_sliced) and
+ * sums in double-double, which is more accurate than the FP64 apply; 0
+ * uses the FP64 apply. */
+#define DPLR_GPU_RESIDUAL_SLICED 1
+#define DPLR_GPU_SOLVE_MIXED 2
+DPLR_API int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *B,
+                               int ldb, double *R, int ldr, int flags, void *stream);
+
+/* Low-precision inner solver for refinement: the Woodbury sweep with V,
+ * the D^-1 W panels and the leaf inverses cut into `slices` bf16 slices
+ * (3 to 6: 22 to 43 bits) on the tensor cores, capacitance inverses
+ * applied in FP64.  More slices cost more tensor-core work per solve but
+ * keep the refinement convergent on worse-conditioned factorisations.
+ * Needs dplr_gpu_factor first and leaf sizes that are multiples of 64. */
+DPLR_API int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream);
+
+/* X := A^-1 B refined until max_j ||B_j - A X_j|| / ||B_j|| <= tol; at
+ * most maxiter corrections.  flags: DPLR_GPU_RESIDUAL_SLICED selects the
+ * exact-slice residual (as for dplr_gpu_residual); DPLR_GPU_SOLVE_MIXED
+ * makes every inner solve the low-precision sweep (needs
+ * dplr_gpu_prepare_mixed) instead of the FP64 sweep.  Reports the final relative residual and the number of
+ * corrections; returns DPLR_GPU_ENOTCONV if the tolerance was not reached. */
 DPLR_API int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb,
-                                    double *X, int ldx, double tol, int maxiter,
+                                    double *X, int ldx, double tol, int maxiter, int flags,
                                     double *rel_resid, int *iters, void *stream);
+
+/* The same refined solve with B and X in host memory (column-major,
+ * leading dimensions ldb, ldx >= m): B is copied to the device, solved and
+ * X copied back inside the call (pinned host memory makes the copies
+ * asynchronous DMA). */
+DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb,
+                                         double *X, int ldx, double tol, int maxiter, int flags,
+                                         double *rel_resid, int *iters, void *stream);
 
 /* Y := alpha*op(A)*X + beta*Y like dplr_gpu_apply, but without allocating
  * any device memory.  No counterpart in DPLR (whose routines malloc per
@@ -93,14 +126,6 @@ DPLR_API int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, 
 DPLR_API int dplr_gpu_apply_noalloc(dplr_gpu_plan plan, char trans, int n, double alpha,
                                     const double *X, int ldx, double beta, double *Y, int ldy,
                                     void *stream);
-
-/* The same refined solve with B and X in host memory (column-major,
- * leading dimensions ldb, ldx >= m): B is copied to the device, solved and
- * X copied back inside the call (pinned host memory makes the copies
- * asynchronous DMA). */
-DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb,
-                                         double *X, int ldx, double tol, int maxiter,
-                                         double *rel_resid, int *iters, void *stream);
 
 /* Instrumentation.  dplr_gpu_launch_count: kernels launched by this
  * library since load.  Between dplr_gpu_profile_start() and

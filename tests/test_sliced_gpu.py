@@ -1,0 +1,131 @@
+"""Exact-slice (bf16 tensor-core) residual R = B - A X.
+
+The residual is checked against one computed in extended precision
+(numpy longdouble on the dense expansion), and shown to be far more
+accurate than the FP64 apply on a matrix with strong cancellation
+(|A||x| >> |b|); refinement with it reaches relative residuals that FP64
+residuals cannot certify.
+"""
+import numpy as np
+import pytest
+
+from dplr_gb300 import gen, tree
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def apply_ld(node, x):
+    """A x from the PLR factors in extended precision (numpy longdouble)."""
+    ld = np.longdouble
+    if isinstance(node, tree.Dense):
+        return node.d.astype(ld) @ x
+    h = node.nw.size
+
+    def lr(b, xs):
+        return (b.u.astype(ld) * b.sig.astype(ld)) @ (b.v.astype(ld).T @ xs)
+    top = apply_ld(node.nw, x[:h]) + lr(node.ne, x[h:])
+    bot = apply_ld(node.se, x[h:]) + lr(node.sw, x[:h])
+    return np.vstack([top, bot])
+
+
+def exact_residual(t, x, b):
+    """b - A x with the PLR operator applied in extended precision."""
+    ax = apply_ld(t, x.astype(np.longdouble).T).T
+    return b.astype(np.longdouble) - ax
+
+
+def _residual_errors(t, x, b):
+    from dplr_gb300.plan import GpuPlan
+    p = GpuPlan(t)
+    p.prepare_sliced()
+    xt = torch.tensor(x, device="cuda")
+    bt = torch.tensor(b, device="cuda")
+    rs = p.residual(xt, bt, precise=True).cpu().numpy()
+    r64 = p.residual(xt, bt, precise=False).cpu().numpy()
+    p.close()
+    want = exact_residual(t, x, b)
+    nb = np.linalg.norm(b)
+    return (float(np.linalg.norm((rs - want).astype(np.float64))) / nb,
+            float(np.linalg.norm((r64 - want).astype(np.float64))) / nb)
+
+
+def test_sliced_residual_on_random_tree():
+    """Diagonally dominant random leaves: both residuals are accurate; the
+    sliced one is never worse than the FP64 apply."""
+    t = gen.random_tree(1024, 64, [24, 16, 8, 4], seed=2)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((6, t.size))
+    b = (tree.to_dense(t) @ x.T).T + 1e-6 * rng.standard_normal((6, t.size))
+    err_s, err_64 = _residual_errors(t, x, b)
+    assert err_s <= 2.0 * err_64 + 1e-18, (err_s, err_64)
+
+
+def test_sliced_residual_under_cancellation():
+    """Kernel matrix with x = A^-1 b: |A||x| >> |b| and the residual cancels
+    across levels.  The exact-slice residual is limited only by the 57-bit
+    slice truncation (about 2^-57 |A||x|), the FP64 apply by rounding in
+    every dot product: the sliced residual must be clearly more accurate."""
+    from dplr_gb300 import gen_gpu
+    from dplr_gb300.plan import GpuPlan
+    t = gen_gpu.kernel_tree_2d(n=4096, leaf=64, shift=1e-2, seed=3, rmax=64)
+    p = GpuPlan(t)
+    p.factor()
+    rng = np.random.default_rng(4)
+    b = rng.standard_normal((6, t.size))
+    x = p.solve(torch.tensor(b, device="cuda")).cpu().numpy()
+    p.close()
+    err_s, err_64 = _residual_errors(t, x, b)
+    assert err_s * 2 <= err_64, (err_s, err_64)
+    assert err_s <= 1e-13, (err_s, err_64)
+
+
+def test_refinement_with_sliced_residual_reaches_1e13():
+    """FP64 inner solves: the FP64 residual stalls near 4e-13 on this
+    matrix, the exact-slice residual certifies 1e-13."""
+    from dplr_gb300 import gen_gpu
+    from dplr_gb300.plan import GpuPlan
+    t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, shift=1e-2, seed=6, rmax=96)
+    p = GpuPlan(t)
+    p.factor()
+    p.prepare_sliced()
+    g = torch.Generator(device="cpu").manual_seed(1)
+    b = torch.randn(16, t.size, generator=g, dtype=torch.float64).cuda()
+    x, res, its = p.solve_refined(b, tol=1e-13, maxiter=10, precise=True)
+    assert res <= 1e-13
+    _, res64, _ = p.solve_refined(b, tol=1e-13, maxiter=4, precise=False, strict=False)
+    assert res64 > res, (res64, res)
+    p.close()
+
+
+@pytest.mark.parametrize("shape", ["kernel2d", "random"])
+def test_mixed_refined_solve_reaches_1e12(shape):
+    """Low-precision (sliced bf16) inner solves + exact-slice residuals.  The
+    kernel matrix needs 6 slices (43 bits): its Woodbury sweep amplifies
+    inner-solve errors by about 1e7."""
+    from dplr_gb300 import gen_gpu
+    from dplr_gb300.plan import GpuPlan
+    from oracle import pyoracle
+    if shape == "kernel2d":
+        t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, seed=6, rmax=96)
+    else:
+        t = gen.random_tree(4096, 64, [32, 24, 16, 8, 4, 2], seed=7)
+    p = GpuPlan(t)
+    p.factor()
+    p.prepare_sliced()
+    p.prepare_mixed(6 if shape == "kernel2d" else 4)
+    b = torch.randn(40, t.size, dtype=torch.float64, device="cuda")
+    x, res, its = p.solve_refined(b, tol=1e-12, maxiter=20, precise=True, mixed=True)
+    assert res <= 1e-12
+    # independent check with the oracle's FP64 apply (its own rounding ~1e-12)
+    orc = pyoracle.oracle("best")
+    a = tree.to_c(t)
+    xb = x.cpu().numpy()
+    y = np.zeros(xb.size)
+    orc.gepdmm("N", "N", t.size, xb.shape[0], 1.0, a, np.ascontiguousarray(xb).reshape(-1), t.size,
+               0.0, y, t.size)
+    tree.free_c(a)
+    bb = b.cpu().numpy()
+    rel = np.max(np.linalg.norm(y.reshape(bb.shape) - bb, axis=1) / np.linalg.norm(bb, axis=1))
+    assert rel <= 1e-11
+    p.close()
