@@ -53,6 +53,15 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("dplr_gpu_solve_refined_host", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
                                                c_double, c_int, c_int, POINTER(c_double),
                                                POINTER(c_int), c_void_p])
+    sig("dplr_gpu_pool_size", c_longlong, [c_void_p])
+    sig("dplr_gpu_pool_blocks", c_int, [c_void_p, POINTER(c_int), POINTER(c_int)])
+    sig("dplr_gpu_pool_block", c_int, [c_void_p, c_int, POINTER(c_longlong), POINTER(c_longlong),
+                                       POINTER(c_longlong), POINTER(c_int), POINTER(c_int),
+                                       POINTER(c_int), POINTER(c_int)])
+    sig("dplr_gpu_pool_read", c_int, [c_void_p, c_void_p, c_void_p])
+    sig("dplr_gpu_pool_write", c_int, [c_void_p, c_void_p, c_void_p])
+    sig("dplr_gpu_grad_factors", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_double,
+                                         c_void_p, c_void_p])
     sig("dplr_gpu_launch_count", c_longlong, [])
     sig("dplr_gpu_profile_start", c_int, [])
     sig("dplr_gpu_profile_stop", c_int, [])

@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
 }
 
 // ---------------------------------------------------------------- reduce
-// T[k, j] = sig[k] * sum_c P[c][k, j]; grid.x = reduce item.
+// T[k, j] = sig[k] * sum_c P[c][k, j] (no scaling with a null sigbase);
+// grid.x = reduce item.
 __global__ void reduce_kernel(const ReduceItem *__restrict__ items,
                               const double *__restrict__ sigbase,
                               const double *__restrict__ partials, int nrhs,
@@ -103,7 +104,7 @@ __global__ void reduce_kernel(const ReduceItem *__restrict__ items,
     const double *P = partials + R.p * nrhs + e;
     double s = 0.0;
     for (int c = 0; c < R.nch; ++c) s += P[(long long)c * cnt];
-    T[R.t * nrhs + e] = R.sig >= 0 ? sigbase[R.sig + k] * s : s;
+    T[R.t * nrhs + e] = (R.sig >= 0 && sigbase) ? sigbase[R.sig + k] * s : s;
 }
 
 // ---------------------------------------------------------------- expand

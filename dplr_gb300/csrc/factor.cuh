@@ -45,6 +45,7 @@ struct Fact {
 
 
 int factor_build(Plan *p, int flags, cudaStream_t st);
+void factor_free(Plan *p);
 int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
                  cudaStream_t st);
 long long factor_bytes(const Plan *p);

@@ -148,6 +148,12 @@ struct Plan {
     void *sliced = nullptr;
     // low-precision sliced solve (sliced.cu)
     void *mixed = nullptr;
+    // error flag of the tensor-core kernels (mapped host memory, sliced.cu)
+    int *tc_err_h = nullptr, *tc_err_d = nullptr;
+    // factor gradients (grad.cu): work lists and scratch
+    void *grad = nullptr;
+    double *gbuf = nullptr;
+    size_t gbuf_doubles = 0;
 };
 
 // plan.cu
@@ -174,6 +180,12 @@ int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int 
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,
                  double beta, double *Y, int ldy, cudaStream_t st, bool alpha0_squares_beta);
 int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream_t st);
+
+// grad.cu
+void grad_free(Plan *p);
+int grad_factors(Plan *p, int nrhs, const double *X, int ldx, const double *DY, int ldy, double alpha, double *G,
+                 cudaStream_t st);
+void plan_values_changed(Plan *p);
 int transpose_device(const double *src, int rows, int cols, int lds, double *dst, int ldd,
                      cudaStream_t st);
 

@@ -388,6 +388,9 @@ void plan_free(Plan *p)
     cudaFree(p->work);
     cudaFree(p->xbuf);
     cudaFree(p->ybuf);
+    if (p->tc_err_h) cudaFreeHost(p->tc_err_h);
+    grad_free(p);
+    cudaFree(p->gbuf);
     delete p;
 }
 

@@ -15,10 +15,12 @@
 // 1e-12 relative residual where an FP64 residual stalls.
 #include "sliced.cuh"
 #include "factor.cuh"
+#include "tcslice.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 
 namespace dg {
 
@@ -62,35 +64,59 @@ __device__ __forceinline__ int scale_exp(double amax)
     return amax > 0.0 ? ilogb(amax) + 1 : 0;
 }
 
-// Slices of y, |y| < 1: a_1 = rint(128 y), then the remainder, 7 bits a slice.
-template <int NS>
-__device__ __forceinline__ void slice_d(double y, bf16 *out, long long stride)
+// round(x * 2^sh) as a 64-bit integer, from the bits of x (integer
+// arithmetic only; the caller keeps |x| 2^sh below 2^62).
+__device__ __forceinline__ long long scaled_int(double x, int sh)
 {
-#pragma unroll
-    for (int p = 0; p < NS; ++p) {
-        double t = y * 128.0;
-        double a = rint(t);
-        y = t - a;                       // exact
-        out[p * stride] = __double2bfloat16(a);
+    const long long bits = __double_as_longlong(x);
+    int ex = (int)((bits >> 52) & 0x7FF);
+    long long m = bits & ((1LL << 52) - 1);
+    if (ex == 0) {
+        if (m == 0) return 0;
+        ex = 1;
+    } else {
+        m |= 1LL << 52;
     }
+    const int s = ex - 1075 + sh;        // |x| 2^sh = m 2^s
+    long long y;
+    if (s >= 0)
+        y = m << s;
+    else if (s <= -54)
+        y = 0;
+    else
+        y = (m + (1LL << (-s - 1))) >> (-s);
+    return bits < 0 ? -y : y;
 }
 
-// Same for a double-double y = hi + lo (|y| < 1).
+// Balanced base-128 digits of y (|y| < 2^(7 NS)): y = sum_p a_p 2^(7 (NS - p)),
+// a_p in [-64, 63] for p > 1 and |a_1| <= 128; written as bf16 (exact).
 template <int NS>
-__device__ __forceinline__ void slice_dd(double hi, double lo, bf16 *out, long long stride)
+__device__ __forceinline__ void int_slices(long long y, bf16 *out, long long stride)
 {
+    int a[NS];
 #pragma unroll
-    for (int p = 0; p < NS; ++p) {
-        double th = hi * 128.0, tl = lo * 128.0;
-        double a = rint(th);
-        double r = th - a;               // exact
-        double s = r + tl;               // two-sum (r, tl)
-        double bb = s - r;
-        double e = (r - (s - bb)) + (tl - bb);
-        hi = s;
-        lo = e;
-        out[p * stride] = __double2bfloat16(a);
+    for (int p = NS - 1; p >= 1; --p) {
+        const long long d = ((y + 64) & 127) - 64;
+        a[p] = (int)d;
+        y = (y - d) >> 7;
     }
+    a[0] = (int)y;
+#pragma unroll
+    for (int p = 0; p < NS; ++p) out[p * stride] = __float2bfloat16_rn((float)a[p]);
+}
+
+// Slices of x with |x| < 2^e: x = 2^e sum_p a_p 2^(-7p) up to 2^(e - 7 NS - 1).
+template <int NS>
+__device__ __forceinline__ void slice_d(double x, int e, bf16 *out, long long stride)
+{
+    int_slices<NS>(scaled_int(x, 7 * NS - e), out, stride);
+}
+
+// Same for a double-double value hi + lo.
+template <int NS>
+__device__ __forceinline__ void slice_dd(double hi, double lo, int e, bf16 *out, long long stride)
+{
+    int_slices<NS>(scaled_int(hi, 7 * NS - e) + scaled_int(lo, 7 * NS - e), out, stride);
 }
 
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
@@ -204,7 +230,7 @@ __global__ void slice_cols_kernel(const SliceJob *jobs, const int *col_base, int
     if (threadIdx.x == 0) exps[J.exp + c] = e;
     for (int i = threadIdx.x; i < J.rows; i += blockDim.x) {
         long long o = J.doff + (long long)c * J.ld + i;
-        slice_d<NS>(ldexp(col[i], -e), dst + o, stride);
+        slice_d<NS>(col[i], e, dst + o, stride);
     }
 }
 
@@ -239,7 +265,7 @@ __global__ void slice_rows_kernel(const RowSliceJob *jobs, const int *row_base, 
     for (int k = 0; k < J.dld; ++k) {
         bf16 *o = dst + J.doff + (long long)r * J.dld + k;
         if (k < J.cols) {
-            slice_d<NS>(ldexp(src[J.off + r + (long long)k * J.ld], -e), o, stride);
+            slice_d<NS>(src[J.off + r + (long long)k * J.ld], e, o, stride);
         } else {
 #pragma unroll
             for (int p = 0; p < NS; ++p) o[p * stride] = zero;
@@ -263,16 +289,23 @@ __global__ void xcol_exp_kernel(const double *X, int m, int ldx, int *xexp)
     if (threadIdx.x == 0) xexp[blockIdx.x] = scale_exp(red[0]);
 }
 
+// One column per blockIdx.y, rows strided over the x-blocks.
 template <int NS>
 __global__ void xslice_kernel(const double *X, int m, int ldx, int nrhs, const int *xexp, bf16 *xs,
                               long long stride)
 {
-    const long long cnt = (long long)m * nrhs;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
-         e += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(e % m), j = (int)(e / m);
-        slice_d<NS>(ldexp(X[i + (long long)j * ldx], -xexp[j]), xs + e, stride);
+    for (int j = blockIdx.y; j < nrhs; j += gridDim.y) {
+        const int e = xexp[j];
+        const double *col = X + (long long)j * ldx;
+        bf16 *out = xs + (long long)j * m;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+            slice_d<NS>(col[i], e, out + i, stride);
     }
+}
+
+static dim3 xslice_grid(int m, int nrhs)
+{
+    return dim3((unsigned)std::max(1, std::min((m + 1023) / 1024, 64)), (unsigned)std::min(nrhs, 65535));
 }
 
 // ------------------------------------------------------------- products
@@ -395,7 +428,7 @@ __global__ void sp_tslice_kernel(const SReduceItem *__restrict__ items, int nite
     const bf16 zero = __float2bfloat16(0.0f);
     for (int k = lane; k < R.rp; k += 32) {
         if (k < R.rank) {
-            slice_dd<NS>(ldexp(th[k], -e), tl ? ldexp(tl[k], -e) : 0.0, out + k, tstride);
+            slice_dd<NS>(th[k], tl ? tl[k] : 0.0, e, out + k, tstride);
         } else {
 #pragma unroll
             for (int p = 0; p < NS; ++p) out[k + p * tstride] = zero;
@@ -527,6 +560,88 @@ constexpr int kD = 9;       // keep pairs p + q <= 9
 
 static long long al32(long long x) { return (x + 31) & ~31LL; }
 static int pad8(int x) { return (x + 7) & ~7; }
+
+// Expand tile height: 128 rows on the tcgen05 kernels when every leaf is a
+// multiple of 128 rows, else 64 rows on the mma.sync kernels.
+// DPLR_GB300_SLICED_MMA=1 selects the mma.sync kernels everywhere.
+static int sliced_tile_rows(const Plan *p)
+{
+    const char *env = std::getenv("DPLR_GB300_SLICED_MMA");
+    if (env && env[0] == '1') return ST;
+    for (const LeafDesc &L : p->leaves)
+        if (L.b % tc::M != 0 || L.row0 % tc::M != 0) return ST;
+    return tc::M;
+}
+
+static int ensure_err_flag(Plan *p)
+{
+    if (p->tc_err_h) return 0;
+    if (cudaHostAlloc((void **)&p->tc_err_h, sizeof(int), cudaHostAllocMapped) != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate the error flag");
+    *p->tc_err_h = 0;
+    if (cudaHostGetDevicePointer((void **)&p->tc_err_d, p->tc_err_h, 0) != cudaSuccess)
+        return fail(DPLR_GPU_ECUDA, "sliced products: cannot map the error flag");
+    return 0;
+}
+
+int sliced_error(Plan *p)
+{
+    if (!p->tc_err_h) return 0;
+    volatile int *f = p->tc_err_h;
+    if (*f == 0) return 0;
+    *f = 0;
+    return fail(DPLR_GPU_ECUDA, "tensor-core slice product: a bounded wait expired");
+}
+
+template <int NS, int D>
+static int tc_attrs()
+{
+    using C = tc::Cfg<NS>;
+    DG_CUDA(cudaFuncSetAttribute(tc::tc_panel_kernel<NS, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    DG_CUDA(cudaFuncSetAttribute(tc::tc_expand_kernel<NS, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    return 0;
+}
+
+// Panel launch of a schedule (tcgen05 or mma.sync kernel).
+template <int NS, int D>
+static void launch_panel(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const bf16 *xs,
+                         long long xstride, int ldx, int nrhs, __int128 *partials, cudaStream_t st)
+{
+    if (S.tile_m == tc::M) {
+        const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
+        const unsigned kt = (unsigned)((S.max_rank + tc::M - 1) / tc::M);
+        tc::tc_panel_kernel<NS, D><<<dim3((unsigned)S.items.size(), rt, kt), tc::THREADS, tc::Cfg<NS>::SMEM, st>>>(
+            S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials, p->tc_err_d);
+    } else {
+        const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
+        sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rt), kSThreads,
+                                     (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
+            S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials);
+    }
+    note_launch();
+}
+
+// Expand launch of a schedule: Y = -/+ sum terms (+ Bin).
+template <int NS, int D>
+static void launch_expand(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
+                          const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, long long xstride,
+                          int ldx, const int *xexp, int nrhs, bool neg, const double *Bin, int ldbin, bool addb,
+                          double *Y, int ldy, cudaStream_t st)
+{
+    const unsigned ntiles = (unsigned)S.tile_row0.size();
+    if (S.tile_m == tc::M) {
+        const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
+        tc::tc_expand_kernel<NS, D><<<dim3(ntiles, rt), tc::THREADS, tc::Cfg<NS>::SMEM, st>>>(
+            S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
+            xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+    } else {
+        const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
+        sp_expand_kernel<NS, NS, D><<<dim3(ntiles, rt), kSThreads, (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
+            S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
+            xexp, nrhs, neg ? -1.0 : 1.0, Bin, ldbin, addb ? 1.0 : 0.0, Y, ldy);
+    }
+    note_launch();
+}
 
 template <class T>
 static int dev_vec(const std::vector<T> &v, T **dst, long long *bytes)
@@ -688,13 +803,14 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
     A.partial_per_rhs = poff;
     A.t_per_rhs = p->total_rank;
     A.tpad_per_rhs = tpad;
-    const int ntiles = p->m / ST;
+    const int TM = A.tile_m = sliced_tile_rows(p);
+    const int ntiles = p->m / TM;
     std::vector<std::vector<STerm>> per(ntiles);
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
         const int rp = pad8(L.rank);
-        for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += ST) {
+        for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += TM) {
             STerm tt;
             tt.a = us_off[b] + (long long)(t0 - L.row0) * rp;
             tt.b = A.reduces[ridx[b]].tpad;
@@ -705,12 +821,12 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
             tt.ldb = rp;
             tt.x_row0 = 0;
             tt.blk = ridx[b];
-            per[t0 / ST].push_back(tt);
+            per[t0 / TM].push_back(tt);
         }
     }
     for (size_t i = 0; i < p->leaves.size(); ++i) {
         const LeafDesc &L = p->leaves[i];
-        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += ST) {
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += TM) {
             STerm tt;
             tt.a = ds_off[i] + (long long)(t0 - L.row0) * L.b;
             tt.b = 0;
@@ -721,21 +837,22 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
             tt.ldb = 0;
             tt.x_row0 = L.row0;
             tt.blk = -1;
-            per[t0 / ST].push_back(tt);
+            per[t0 / TM].push_back(tt);
         }
     }
     for (int t = 0; t < ntiles; ++t) {
-        A.tile_row0.push_back(t * ST);
+        A.tile_row0.push_back(t * TM);
         A.tile_begin.push_back((int)A.terms.size());
         A.terms.insert(A.terms.end(), per[t].begin(), per[t].end());
     }
     A.tile_begin.push_back((int)A.terms.size());
     if ((rc = upload_sschedule(A, &S->bytes))) return rc;
+    if ((rc = ensure_err_flag(p))) return rc;
     DG_CUDA(cudaFuncSetAttribute(sp_panel_kernel<kNS, kNS, kD>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
     DG_CUDA(cudaFuncSetAttribute(sp_expand_kernel<kNS, kNS, kD>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
-    return 0;
+    return tc_attrs<kNS, kD>();
 }
 
 // Scratch of one sliced apply with nrhs columns: X slices, exponents,
@@ -767,10 +884,11 @@ static int sliced_scratch(Sliced *S, const SSchedule &A, int m, int nrhs, int ns
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
         S->xexp_n = nrhs;
     }
-    const size_t part_bytes = (size_t)A.partial_per_rhs * nrhs * sizeof(__int128);
-    const size_t t_bytes = (size_t)2 * A.t_per_rhs * nrhs * sizeof(double);
+    auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t part_bytes = r256((size_t)A.partial_per_rhs * nrhs * sizeof(__int128));
+    const size_t t_bytes = r256((size_t)2 * A.t_per_rhs * nrhs * sizeof(double));
     const size_t ts_elems = (size_t)A.tpad_per_rhs * nrhs;
-    const size_t ts_bytes = ((size_t)ns * ts_elems * sizeof(bf16) + 255) & ~(size_t)255;
+    const size_t ts_bytes = r256((size_t)ns * ts_elems * sizeof(bf16));
     const size_t te_bytes = (size_t)A.reduces.size() * nrhs * sizeof(int);
     const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes + 1024;
     if (S->work_bytes < need) {
@@ -807,14 +925,10 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
         ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * kNS * m * nrhs);
         xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, S->xexp);
         note_launch();
-        long long cnt = (long long)m * nrhs;
-        int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
-        xslice_kernel<kNS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, S->xexp, S->xs, xstride);
+        xslice_kernel<kNS><<<xslice_grid(m, nrhs), 256, 0, st>>>(X, m, ldx, nrhs, S->xexp, S->xs, xstride);
         note_launch();
         DG_CUDA(cudaGetLastError());
     }
-    const unsigned rtiles = (unsigned)((nrhs + ST - 1) / ST);
-    const size_t smem = panel_smem(kNS, kNS);
     int npairs = 0;
     for (int d = 2; d <= kD; ++d)
         for (int pp = std::max(1, d - kNS); pp <= std::min(kNS, d - 1); ++pp) ++npairs;
@@ -826,9 +940,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
         }
         {
             ProfScope ps("sliced_panel", st, fl * npairs, by);
-            sp_panel_kernel<kNS, kNS, kD><<<dim3((unsigned)A.items.size(), rtiles), kSThreads, smem, st>>>(
-                A.d_items, S->pool, S->stride, S->xs, xstride, m, nrhs, w.partials);
-            note_launch();
+            launch_panel<kNS, kD>(p, A, S->pool, S->stride, S->xs, xstride, m, nrhs, w.partials, st);
             DG_CUDA(cudaGetLastError());
         }
         ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
@@ -842,18 +954,15 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
         note_launch();
         DG_CUDA(cudaGetLastError());
     }
-    const unsigned ntiles = (unsigned)A.tile_row0.size();
-    if (ntiles) {
+    if (!A.tile_row0.empty()) {
         double fl = 0, by = 0;
         for (const STerm &t : A.terms) {
-            fl += 2.0 * ST * t.K * nrhs;
-            by += 2.0 * kNS * ((double)ST * t.K) + 2.0 * kNS * t.K * nrhs;
+            fl += 2.0 * A.tile_m * t.K * nrhs;
+            by += 2.0 * kNS * ((double)A.tile_m * t.K) + 2.0 * kNS * t.K * nrhs;
         }
         ProfScope ps("sliced_expand", st, fl * npairs, by + 16.0 * m * nrhs);
-        sp_expand_kernel<kNS, kNS, kD><<<dim3(ntiles, rtiles), kSThreads, smem, st>>>(
-            A.d_terms, A.d_tile_row0, A.d_tile_begin, S->pool, S->stride, S->exps, w.ts, w.tstride,
-            w.texp, S->xs, xstride, m, S->xexp, nrhs, -1.0, B, ldb, 1.0, R, ldr);
-        note_launch();
+        launch_expand<kNS, kD>(p, A, S->pool, S->stride, S->exps, w.ts, w.tstride, w.texp, S->xs, xstride, m,
+                               S->xexp, nrhs, true, B, ldb, true, R, ldr, st);
         DG_CUDA(cudaGetLastError());
     }
     return 0;
@@ -937,6 +1046,7 @@ static int mixed_slice_t(const std::vector<SliceJob> &vj, const std::vector<int>
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(NS, NS));
         if (e3 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "mixed solve: %s", cudaGetErrorString(e3));
     }
+    if (!rc) rc = tc_attrs<NS, NS + 1>();
 out:
     cudaFree(d_vj);
     cudaFree(d_vb);
@@ -1025,8 +1135,11 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
     M->t_per_rhs = p->total_rank;
     M->nblocks = (int)p->lr.size();
     M->level.resize(nlev);
+    const int TM = sliced_tile_rows(p);
+    if ((rc = ensure_err_flag(p))) return rc;
     for (int l = 0; l < nlev; ++l) {
         SSchedule &S = M->level[l];
+        S.tile_m = TM;
         long long poff = 0;
         const int wp = pad8(F->lv[l].width);
         for (int b : F->lv[l].blocks) {
@@ -1049,7 +1162,7 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
             S.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], pad8(L.rank), tpad[b]});
             poff += (long long)nch * L.rank;
             S.max_rank = std::max(S.max_rank, L.rank);
-            for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += ST) {
+            for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += TM) {
                 STerm tt;
                 tt.a = zs_off[l] + (long long)t0 * wp;
                 tt.b = tpad[b];
@@ -1072,9 +1185,10 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
         if ((rc = upload_sschedule(S, &M->bytes))) return rc;
     }
     SSchedule &LS = M->leaf;
+    LS.tile_m = TM;
     for (size_t i = 0; i < p->leaves.size(); ++i) {
         const LeafDesc &L = p->leaves[i];
-        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += ST) {
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += TM) {
             STerm tt;
             tt.a = ls_off[i] + (long long)(t0 - L.row0) * L.b;
             tt.b = 0;
@@ -1100,9 +1214,7 @@ static int slice_block(const double *X, int m, int ldx, int nrhs, bf16 *xs, int 
 {
     xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, xexp);
     note_launch();
-    long long cnt = (long long)m * nrhs;
-    int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
-    xslice_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xexp, xs, (long long)m * nrhs);
+    xslice_kernel<NS><<<xslice_grid(m, nrhs), 256, 0, st>>>(X, m, ldx, nrhs, xexp, xs, (long long)m * nrhs);
     note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
@@ -1138,10 +1250,12 @@ static int mixed_scratch(MixedSliced *M, int m, int nrhs, MWork &w)
     }
     long long part = 0;
     for (const SSchedule &L : M->level) part = std::max(part, L.partial_per_rhs);
-    const size_t part_bytes = (size_t)part * nrhs * sizeof(__int128);
-    const size_t t_bytes = (size_t)2 * M->t_per_rhs * nrhs * sizeof(double);
-    const size_t w_bytes = (size_t)M->t_per_rhs * nrhs * sizeof(double);
-    const size_t ws_bytes = ((size_t)M->ns * M->tpad_per_rhs * nrhs * sizeof(bf16) + 255) & ~(size_t)255;
+    // every carve starts on a 256-byte boundary (16-byte copies need it)
+    auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t part_bytes = r256((size_t)part * nrhs * sizeof(__int128));
+    const size_t t_bytes = r256((size_t)2 * M->t_per_rhs * nrhs * sizeof(double));
+    const size_t w_bytes = r256((size_t)M->t_per_rhs * nrhs * sizeof(double));
+    const size_t ws_bytes = r256((size_t)M->ns * M->tpad_per_rhs * nrhs * sizeof(bf16));
     size_t maxred = 0;
     for (const SSchedule &L : M->level) maxred = std::max(maxred, L.reduces.size());
     const size_t we_bytes = std::max<size_t>(maxred, 1) * nrhs * sizeof(int);
@@ -1175,8 +1289,6 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
     int rc = mixed_scratch(M, m, nrhs, w);
     if (rc) return rc;
     const long long xstride = (long long)m * nrhs;
-    const unsigned rtiles = (unsigned)((nrhs + ST - 1) / ST);
-    const size_t smem = panel_smem(NS, NS);
     const double npairs = pair_count(NS, D);
 
     // leaf step: X = Leaf^-1 B
@@ -1184,12 +1296,10 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
     {
         const SSchedule &LS = M->leaf;
         double fl = 0;
-        for (const STerm &t : LS.terms) fl += 2.0 * ST * t.K * nrhs;
+        for (const STerm &t : LS.terms) fl += 2.0 * LS.tile_m * t.K * nrhs;
         ProfScope ps("mixed_expand", st, fl * npairs, 0.0);
-        sp_expand_kernel<NS, NS, D><<<dim3((unsigned)LS.tile_row0.size(), rtiles), kSThreads, smem, st>>>(
-            LS.d_terms, LS.d_tile_row0, LS.d_tile_begin, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp,
-            M->xs, xstride, m, M->xexp, nrhs, 1.0, nullptr, 0, 0.0, X, ldx);
-        note_launch();
+        launch_expand<NS, D>(p, LS, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp, M->xs, xstride, m,
+                             M->xexp, nrhs, false, nullptr, 0, false, X, ldx, st);
         DG_CUDA(cudaGetLastError());
     }
     for (int l = (int)M->level.size() - 1; l >= 0; --l) {
@@ -1200,9 +1310,7 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
         for (const SPanelItem &it : S.items) fl += 2.0 * it.len * it.rank * nrhs;
         {
             ProfScope ps("mixed_panel", st, fl * npairs, 0.0);
-            sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rtiles), kSThreads, smem, st>>>(
-                S.d_items, M->pool, M->stride, M->xs, xstride, m, nrhs, w.partials);
-            note_launch();
+            launch_panel<NS, D>(p, S, M->pool, M->stride, M->xs, xstride, m, nrhs, w.partials, st);
         }
         long long maxcnt = (long long)S.max_rank * nrhs;
         sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
@@ -1216,12 +1324,10 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
             S.d_reduces, (int)S.reduces.size(), w.W, -1, nrhs, w.ws, w.wstride, w.wexp);
         note_launch();
         double fu = 0;
-        for (const STerm &t : S.terms) fu += 2.0 * ST * t.K * nrhs;
+        for (const STerm &t : S.terms) fu += 2.0 * S.tile_m * t.K * nrhs;
         ProfScope ps2("mixed_expand", st, fu * npairs, 0.0);
-        sp_expand_kernel<NS, NS, D><<<dim3((unsigned)S.tile_row0.size(), rtiles), kSThreads, smem, st>>>(
-            S.d_terms, S.d_tile_row0, S.d_tile_begin, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp,
-            M->xs, xstride, m, M->xexp, nrhs, -1.0, X, ldx, 1.0, X, ldx);
-        note_launch();
+        launch_expand<NS, D>(p, S, M->pool, M->stride, M->exps, w.ws, w.wstride, w.wexp, M->xs, xstride, m,
+                             M->xexp, nrhs, true, X, ldx, true, X, ldx, st);
         DG_CUDA(cudaGetLastError());
     }
     return 0;

@@ -55,6 +55,7 @@ struct STerm {
 };
 
 struct SSchedule {
+    int tile_m = 64;                // rows of an expand tile: 64 (mma.sync) or 128 (tcgen05)
     std::vector<SPanelItem> items;
     std::vector<SReduceItem> reduces;
     long long partial_per_rhs = 0;
@@ -116,6 +117,9 @@ void mixed_free(Plan *p);
 int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx, cudaStream_t st);
 
 int sliced_build(Plan *p, int ns, cudaStream_t st);
+// Error recorded by a tensor-core kernel whose bounded wait expired (the
+// flag is cleared); 0 if none.
+int sliced_error(Plan *p);
 void sliced_free(Plan *p);
 // R = B - A X with exact-slice products (8 slices: FP64-or-better accuracy).
 int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B, int ldb,

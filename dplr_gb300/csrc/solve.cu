@@ -120,6 +120,8 @@ int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int ldx, const
     if (n < 0 || ldx < mm || ldb < mm || ldr < mm)
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_residual: invalid n or leading dimension");
     cudaStream_t st = (cudaStream_t)stream;
+    int rc0 = sliced_error(p);          // reported by an earlier asynchronous call
+    if (rc0) return rc0;
     if (flags & DPLR_GPU_RESIDUAL_SLICED) return sliced_residual(p, n, X, ldx, B, ldb, R, ldr, st);
     int rc = axpby_device(p->m, n, 1.0, B, ldb, 0.0, R, ldr, st);
     if (rc) return rc;
@@ -172,6 +174,7 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
         if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
         DG_CUDA(cudaMemcpyAsync(hr.data(), rn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         DG_CUDA(cudaStreamSynchronize(st));
+        if ((rc = sliced_error(p))) return rc;
         worst = 0.0;
         for (int j = 0; j < n; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
         if (worst <= tol || it >= maxiter) break;

@@ -49,6 +49,7 @@ class GpuPlan:
                                ctypes.byref(mr))
         self.nnz, self.levels, self.max_rank = nnz.value, lev.value, mr.value
         self.factored = False
+        self.factored_transposed = False
         self.sliced = False
         self.mixed = False
 
@@ -115,11 +116,72 @@ class GpuPlan:
                                                    _stream_ptr(stream)), "dplr_gpu_apply")
         return out
 
+    # -------------------------------------------------------------- factor pool
+    def pool_size(self) -> int:
+        return int(_native.lib().dplr_gpu_pool_size(self._h))
+
+    def read_pool(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """Device copy of every factor value (pool layout, float64)."""
+        n = self.pool_size()
+        out = torch.empty(n, dtype=torch.float64, device="cuda") if out is None else out
+        if not (out.is_cuda and out.dtype == torch.float64 and out.is_contiguous() and out.numel() == n):
+            raise ValueError(f"pool tensor must be a contiguous CUDA float64 tensor of {n} elements")
+        _native.check(_native.lib().dplr_gpu_pool_read(self._h, out.data_ptr(), _stream_ptr(stream)),
+                      "dplr_gpu_pool_read")
+        return out
+
+    def write_pool(self, values: torch.Tensor, stream=None) -> None:
+        """Replace the factor values (same structure); the factorisation and
+        sliced copies must be rebuilt afterwards."""
+        n = self.pool_size()
+        if not (values.is_cuda and values.dtype == torch.float64 and values.is_contiguous()
+                and values.numel() == n):
+            raise ValueError(f"pool tensor must be a contiguous CUDA float64 tensor of {n} elements")
+        _native.check(_native.lib().dplr_gpu_pool_write(self._h, values.data_ptr(), _stream_ptr(stream)),
+                      "dplr_gpu_pool_write")
+        self.factored = self.factored_transposed = self.sliced = self.mixed = False
+
+    def pool_blocks(self) -> list[dict]:
+        """Layout of the pool: low-rank blocks (pre-order, ne before sw), then
+        leaves; offsets in doubles."""
+        lib = _native.lib()
+        nlr, nlf = ctypes.c_int(), ctypes.c_int()
+        _native.check(lib.dplr_gpu_pool_blocks(self._h, ctypes.byref(nlr), ctypes.byref(nlf)),
+                      "dplr_gpu_pool_blocks")
+        out = []
+        u, v, sg = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        n, r, r0, c0 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        for i in range(nlr.value + nlf.value):
+            _native.check(lib.dplr_gpu_pool_block(self._h, i, ctypes.byref(u), ctypes.byref(v),
+                                                  ctypes.byref(sg), ctypes.byref(n), ctypes.byref(r),
+                                                  ctypes.byref(r0), ctypes.byref(c0)),
+                          "dplr_gpu_pool_block")
+            if i < nlr.value:
+                out.append({"kind": "lowrank", "u": u.value, "v": v.value, "sig": sg.value,
+                            "n": n.value, "rank": r.value, "row0": r0.value, "col0": c0.value})
+            else:
+                out.append({"kind": "leaf", "d": u.value, "b": n.value, "row0": r0.value})
+        return out
+
+    def grad_factors(self, x: torch.Tensor, dy: torch.Tensor, alpha: float = 1.0,
+                     out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """out (pool layout) += alpha * d<dy, A x>/d(factors)."""
+        _check_block(x, self.m, "x")
+        _check_block(dy, self.m, "dy")
+        if x.shape[0] != dy.shape[0]:
+            raise ValueError("x and dy must have the same number of columns")
+        out = torch.zeros(self.pool_size(), dtype=torch.float64, device="cuda") if out is None else out
+        _native.check(_native.lib().dplr_gpu_grad_factors(self._h, x.shape[0], x.data_ptr(), self.m,
+                                                          dy.data_ptr(), self.m, alpha, out.data_ptr(),
+                                                          _stream_ptr(stream)), "dplr_gpu_grad_factors")
+        return out
+
     # -------------------------------------------------------------- solve
     def factor(self, transposed: bool = False, stream=None) -> None:
         _native.check(_native.lib().dplr_gpu_factor(self._h, 1 if transposed else 0,
                                                     _stream_ptr(stream)), "dplr_gpu_factor")
         self.factored = True
+        self.factored_transposed = bool(transposed)
 
     def solve(self, b: torch.Tensor, trans: str = "N", out: torch.Tensor | None = None,
               stream=None) -> torch.Tensor:

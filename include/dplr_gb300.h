@@ -127,6 +127,35 @@ DPLR_API int dplr_gpu_apply_noalloc(dplr_gpu_plan plan, char trans, int n, doubl
                                     const double *X, int ldx, double beta, double *Y, int ldy,
                                     void *stream);
 
+/* Factor pool.  A plan holds every factor in one device FP64 array of
+ * dplr_gpu_pool_size() doubles.  Its blocks are numbered 0 .. nlowrank-1
+ * for the low-rank blocks (pre-order over the tree, ne before sw) and
+ * nlowrank .. nlowrank+nleaves-1 for the dense leaves (left to right);
+ * dplr_gpu_pool_block() gives a block's offsets in the pool (U, V: n x rank
+ * column-major, ld n; sig: rank; a leaf's b x b matrix at *u, ld b, with
+ * *v = *sig = -1), its size, rank and the rows it writes (row0) and reads
+ * (col0) in the op-N product.  No counterpart in DPLR, whose factors live
+ * in the host tree. */
+DPLR_API long long dplr_gpu_pool_size(dplr_gpu_plan plan);
+DPLR_API int dplr_gpu_pool_blocks(dplr_gpu_plan plan, int *nlowrank, int *nleaves);
+DPLR_API int dplr_gpu_pool_block(dplr_gpu_plan plan, int i, long long *u, long long *v, long long *sig,
+                                 int *n, int *rank, int *row0, int *col0);
+/* Device-to-device copies of the pool.  Writing replaces the factor values
+ * (same structure) and drops the factorisation and sliced copies built from
+ * the old values. */
+DPLR_API int dplr_gpu_pool_read(dplr_gpu_plan plan, double *dst, void *stream);
+DPLR_API int dplr_gpu_pool_write(dplr_gpu_plan plan, const double *src, void *stream);
+
+/* Adjoint of the product with respect to the factors: G (device, pool
+ * layout) += alpha * d<DY, A X>/d(factors), i.e. per low-rank block
+ * dU = DY_R (sig o V^T X_C)^T, dV = X_C (sig o U^T DY_R)^T,
+ * dsig = rowsum((U^T DY_R) o (V^T X_C)), per leaf dD = DY_R X_R^T (R, C: the
+ * block's row and column ranges).  With X = A^-1 B and DY = A^-T G_X,
+ * alpha = -1 gives the factor gradient of a solve.  X, DY: m x n device
+ * arrays.  No counterpart in DPLR. */
+DPLR_API int dplr_gpu_grad_factors(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *DY,
+                                   int ldy, double alpha, double *G, void *stream);
+
 /* Instrumentation.  dplr_gpu_launch_count: kernels launched by this
  * library since load.  Between dplr_gpu_profile_start() and
  * dplr_gpu_profile_stop() the main kernels are bracketed by CUDA events on

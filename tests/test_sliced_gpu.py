@@ -129,3 +129,72 @@ def test_mixed_refined_solve_reaches_1e12(shape):
     rel = np.max(np.linalg.norm(y.reshape(bb.shape) - bb, axis=1) / np.linalg.norm(bb, axis=1))
     assert rel <= 1e-11
     p.close()
+
+
+def _plan(t, mma: bool, mixed_slices: int = 0):
+    """Plan whose sliced products run on the mma.sync kernels (mma=True) or
+    on the tcgen05 kernels (128-row tiles; leaves must be multiples of 128)."""
+    import os
+    from dplr_gb300.plan import GpuPlan
+    old = os.environ.get("DPLR_GB300_SLICED_MMA")
+    os.environ["DPLR_GB300_SLICED_MMA"] = "1" if mma else "0"
+    try:
+        p = GpuPlan(t)
+        p.factor()
+        p.prepare_sliced()
+        if mixed_slices:
+            p.prepare_mixed(mixed_slices)
+    finally:
+        if old is None:
+            del os.environ["DPLR_GB300_SLICED_MMA"]
+        else:
+            os.environ["DPLR_GB300_SLICED_MMA"] = old
+    return p
+
+
+@pytest.mark.parametrize("kind", ["random_rank160", "kernel2d"])
+def test_tcgen05_residual_matches_mma_sync(kind):
+    """Both kernel families compute the same exact integer products; the
+    tcgen05 expand rounds its exact fixed-point sum once, the mma.sync
+    expand accumulates in double-double: results agree to an ulp.  70
+    right-hand sides exercise a ragged 64-column tile; ranks above 128
+    exercise the panel's second rank tile."""
+    from dplr_gb300 import gen_gpu
+    if kind == "kernel2d":
+        t = gen_gpu.kernel_tree_2d(n=8192, leaf=128, rmax=96, seed=8)
+    else:
+        t = gen.random_tree(2048, 128, [160, 140, 100, 40], seed=9)
+    rng = np.random.default_rng(10)
+    x = rng.standard_normal((70, t.size))
+    b = rng.standard_normal((70, t.size))
+    pt, pm = _plan(t, mma=False), _plan(t, mma=True)
+    xt = torch.tensor(x, device="cuda")
+    bt = torch.tensor(b, device="cuda")
+    rt = pt.residual(xt, bt, precise=True).cpu().numpy()
+    rm = pm.residual(xt, bt, precise=True).cpu().numpy()
+    pt.close()
+    pm.close()
+    assert np.all(np.isfinite(rt))
+    ulp = np.spacing(np.maximum(np.abs(rt), np.abs(rm)))
+    assert np.all(np.abs(rt - rm) <= 2 * ulp + 1e-300), float(np.max(np.abs(rt - rm) / ulp))
+    want = exact_residual(t, x, b)
+    nax = float(np.linalg.norm((b - want).astype(np.float64)))      # ||A x||
+    err_t = float(np.linalg.norm((rt - want).astype(np.float64))) / nax
+    assert err_t <= 1e-15, err_t
+
+
+def test_tcgen05_mixed_refined_solve():
+    """Mixed refinement with the tcgen05 kernels reaches the tolerance and
+    agrees with the mma.sync path's solution."""
+    from dplr_gb300 import gen_gpu
+    t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, rmax=96, seed=6)
+    g = torch.Generator(device="cpu").manual_seed(2)
+    b = torch.randn(70, t.size, generator=g, dtype=torch.float64).cuda()
+    pt, pm = _plan(t, mma=False, mixed_slices=6), _plan(t, mma=True, mixed_slices=6)
+    xt, rt, _ = pt.solve_refined(b, tol=1e-12, maxiter=10, precise=True, mixed=True)
+    xm, rm, _ = pm.solve_refined(b, tol=1e-12, maxiter=10, precise=True, mixed=True)
+    pt.close()
+    pm.close()
+    assert rt <= 1e-12 and rm <= 1e-12, (rt, rm)
+    rel = float(((xt - xm).norm(dim=1) / xm.norm(dim=1)).max())
+    assert rel <= 1e-9, rel
