@@ -57,6 +57,9 @@ def parse():
                     help="bf16 slices of the mixed inner solve (3 to 6)")
     ap.add_argument("--residual", choices=["sliced", "fp64"], default="sliced",
                     help="refinement residual: exact-slice tensor-core products or the FP64 apply")
+    ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint"], default="solve",
+                    help="solve: the headline refined solve; the others are secondary workloads "
+                         "(dplr_gb300/workloads.py)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-sample", type=int, default=1 << 14,
                     help="size of the diagonal sub-block the CPU baseline runs on")
@@ -487,10 +490,38 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_secondary(args):
+    """Secondary workloads on one GPU (replicas under torchrun: rank 0 reports)."""
+    import torch
+    from dplr_gb300 import workloads
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    sampler = ClockSampler(local)
+    if args.workload == "apply":
+        t, stats = build_matrix(args, device=f"cuda:{local}")
+        from dplr_gb300.plan import GpuPlan
+        plan = GpuPlan(t)
+        sampler.start()
+        out = workloads.apply_workload(plan, args.n, max(args.steps, 10), args.warmup, ROOT)
+    elif args.workload == "batched":
+        sampler.start()
+        out = workloads.batched_workload(max(args.steps, 10), args.warmup)
+    else:
+        sampler.start()
+        out = workloads.adjoint_workload(max(args.steps, 5), args.warmup)
+    out["clocks"] = sampler.stop()
+    out.update({"n_gpus": 1, "steps": max(args.steps, 10), "warmup": max(3, args.warmup), "scaling": "weak",
+                "vs_baseline": None, "data": "synthetic"})
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "solve":
+        run_secondary(args)
     else:
         run_ours(args)
 

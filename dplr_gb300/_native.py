@@ -62,6 +62,16 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("dplr_gpu_pool_write", c_int, [c_void_p, c_void_p, c_void_p])
     sig("dplr_gpu_grad_factors", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_double,
                                          c_void_p, c_void_p])
+    sig("dplr_gpu_batch_create", c_int, [c_int, POINTER(c_int), POINTER(PDPlrMtx), c_void_p,
+                                         POINTER(c_void_p)])
+    sig("dplr_gpu_batch_offsets", c_int, [c_void_p, POINTER(c_int), POINTER(c_int)])
+    sig("dplr_gpu_graph_create", c_int, [c_void_p, c_char, c_char, c_int, c_void_p, c_int, c_void_p,
+                                         c_int, c_void_p, POINTER(c_void_p)])
+    sig("dplr_gpu_graph_launch", c_int, [c_void_p, c_void_p])
+    sig("dplr_gpu_graph_kernels", c_longlong, [c_void_p])
+    sig("dplr_gpu_graph_destroy", None, [c_void_p])
+    sig("dplr_gpu_autotune", c_int, [c_void_p, c_int, c_void_p, POINTER(c_int), POINTER(c_int),
+                                     POINTER(c_double)])
     sig("dplr_gpu_launch_count", c_longlong, [])
     sig("dplr_gpu_profile_start", c_int, [])
     sig("dplr_gpu_profile_stop", c_int, [])

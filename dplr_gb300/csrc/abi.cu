@@ -276,6 +276,7 @@ struct ProfAgg {
 static std::vector<ProfAgg> g_prof_out;
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 ProfScope::ProfScope(const char *name, cudaStream_t st, double flops, double bytes)
 {

@@ -306,9 +306,10 @@ int transpose_device(const double *src, int rows, int cols, int lds, double *dst
     return 0;
 }
 
-static int pick_nb(int nrhs)
+static int pick_nb(int nrhs, int cap = 16)
 {
-    return nrhs >= 16 ? 16 : nrhs >= 8 ? 8 : nrhs >= 4 ? 4 : nrhs >= 2 ? 2 : 1;
+    const int nb = nrhs >= 16 ? 16 : nrhs >= 8 ? 8 : nrhs >= 4 ? 4 : nrhs >= 2 ? 2 : 1;
+    return std::min(nb, std::max(cap, 1));
 }
 
 #define DG_DISPATCH_NB(nb, CALL)                                                   \
@@ -324,7 +325,7 @@ int run_panel(const Schedule &S, const double *fbase, const double *X, int ldx, 
               double *partials, cudaStream_t st)
 {
     if (S.items.empty() || nrhs <= 0) return 0;
-    const int nb = pick_nb(nrhs);
+    const int nb = pick_nb(nrhs, S.nb_cap);
     dim3 g((unsigned)S.items.size(), (unsigned)((nrhs + nb - 1) / nb));
     double fl = 0, by = 0;
     for (const PanelItem &it : S.items) {
@@ -362,7 +363,7 @@ int run_expand(const Schedule &S, const double *abase, const double *T, const do
 {
     const int ntiles = (int)S.tile_row0.size();
     if (ntiles == 0 || nrhs <= 0) return 0;
-    const int nb = pick_nb(nrhs);
+    const int nb = pick_nb(nrhs, S.nb_cap);
     dim3 g(ntiles, (unsigned)((nrhs + nb - 1) / nb));
     double fl = 0, by = 8.0 * ntiles * S.tile_rows * nrhs * (beta == 0.0 ? 1.0 : 2.0);
     for (const TileTerm &t : S.terms) {

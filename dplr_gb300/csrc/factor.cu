@@ -323,6 +323,7 @@ static void build_level_schedules(Plan *p, Fact *F)
             S.t_per_rhs = p->total_rank;
             S.max_rank = maxr;
             S.tile_rows = R;
+            S.nb_cap = p->nb_cap;
             for (int nd : L.nodes) {
                 const HDesc &H = p->nodes[nd];
                 const LRDesc &ne = p->lr[H.ne], &sw = p->lr[H.sw];
@@ -343,6 +344,7 @@ static void build_level_schedules(Plan *p, Fact *F)
     for (int trans = 0; trans < 2; ++trans) {
         Schedule &S = trans ? F->leafT : F->leafN;
         S.tile_rows = R;
+        S.nb_cap = p->nb_cap;
         for (size_t i = 0; i < p->leaves.size(); ++i) {
             const LeafDesc &Lf = p->leaves[i];
             for (int t0 = Lf.row0; t0 < Lf.row0 + Lf.b; t0 += R) {

@@ -38,6 +38,7 @@ int fail(int code, const char *fmt, ...);
 // launching stream and record the algorithmic flops and bytes of that
 // launch (see prof_begin / prof_end in abi.cu).
 void note_launch();
+void note_launches(long long k);
 struct ProfScope {
     int id = -1;
     cudaStream_t stream_ = nullptr;
@@ -117,6 +118,7 @@ struct Schedule {
     std::vector<CapItem> caps;
     int tile_rows = 0;
     int max_rank = 0;
+    int nb_cap = 16;                  // largest right-hand-side tile (autotuned)
     PanelItem *d_items = nullptr;
     ReduceItem *d_reduces = nullptr;
     int *d_tile_row0 = nullptr, *d_tile_begin = nullptr;
@@ -126,6 +128,9 @@ struct Schedule {
 
 struct Plan {
     int m = 0, levels = 0, max_rank = 0, total_rank = 0;
+    int ntrees = 1;                   // > 1: a batch of independent trees (block diagonal)
+    std::vector<int> tree_row0;       // first row of every tree
+    int nb_cap = 16;                  // largest right-hand-side tile of the FP64 kernels (autotuned)
     long long nnz = 0;
     std::vector<LRDesc> lr;
     std::vector<LeafDesc> leaves;
@@ -158,6 +163,8 @@ struct Plan {
 
 // plan.cu
 int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out);
+int plan_build_forest(int count, const int *ms, const DPlrMtx *const *As, cudaStream_t st, Plan **out);
+int plan_reschedule(Plan *p);
 int plan_upload_values(Plan *p, const DPlrMtx *A, cudaStream_t st);
 void plan_free(Plan *p);
 int ensure_buffer(double **buf, size_t *have, size_t need);

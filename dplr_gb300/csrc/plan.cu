@@ -304,6 +304,7 @@ struct Uploader {
 
 int plan_upload_values(Plan *p, const DPlrMtx *A, cudaStream_t st)
 {
+    if (p->ntrees != 1) return fail(DPLR_GPU_EINVAL, "plan refresh: batched plans are refreshed through the pool");
     if (!A || A->size != p->m) return fail(DPLR_GPU_EINVAL, "plan refresh: size mismatch");
     int rc = validate_tree(p->m, A, "dplr_gpu_plan_refresh");
     if (rc) return rc;
@@ -318,12 +319,32 @@ int plan_upload_values(Plan *p, const DPlrMtx *A, cudaStream_t st)
 
 int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out)
 {
-    int rc = validate_tree(m, A, "dplr_gpu_plan_create");
-    if (rc) return rc;
+    return plan_build_forest(1, &m, &A, st, out);
+}
+
+// A forest of independent trees as one block-diagonal matrix: tree i owns
+// rows [sum_{k<i} m_k, sum_{k<=i} m_k).  Blocks and leaves of all trees go
+// into the same tables, so every phase covers all trees in one launch.
+int plan_build_forest(int count, const int *ms, const DPlrMtx *const *As, cudaStream_t st, Plan **out)
+{
+    int rc;
+    long long total = 0;
+    for (int i = 0; i < count; ++i) {
+        if ((rc = validate_tree(ms[i], As[i], count == 1 ? "dplr_gpu_plan_create" : "dplr_gpu_batch_create")))
+            return rc;
+        total += ms[i];
+    }
+    if (total > (1LL << 31) - 1) return fail(DPLR_GPU_EINVAL, "plan: %lld rows exceed the int range", total);
     Plan *p = new Plan();
-    p->m = m;
+    p->m = (int)total;
+    p->ntrees = count;
     Builder b{p};
-    b.walk(A, 0, 0);
+    int row0 = 0;
+    for (int i = 0; i < count; ++i) {
+        p->tree_row0.push_back(row0);
+        b.walk(As[i], row0, 0);
+        row0 += ms[i];
+    }
     build_schedule(p, 0, p->sched[0]);
     build_schedule(p, 1, p->sched[1]);
     long long bytes = 0;
@@ -342,7 +363,7 @@ int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out)
     }
     p->device_bytes = bytes;
     Uploader up{p, st};
-    rc = up.walk(A);
+    for (int i = 0; i < count && !rc; ++i) rc = up.walk(As[i]);
     if (!rc) {
         cudaError_t e2 = cudaStreamSynchronize(st);
         if (e2 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "plan upload: %s", cudaGetErrorString(e2));
@@ -352,6 +373,19 @@ int plan_build(int m, const DPlrMtx *A, cudaStream_t st, Plan **out)
         return rc;
     }
     *out = p;
+    return 0;
+}
+
+// Rebuild the apply schedules (after a change of the panel chunk length).
+int plan_reschedule(Plan *p)
+{
+    long long bytes = 0;
+    free_schedule(p->sched[0]);
+    free_schedule(p->sched[1]);
+    build_schedule(p, 0, p->sched[0]);
+    build_schedule(p, 1, p->sched[1]);
+    int rc;
+    if ((rc = upload_schedule(p->sched[0], &bytes)) || (rc = upload_schedule(p->sched[1], &bytes))) return rc;
     return 0;
 }
 

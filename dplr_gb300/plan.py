@@ -28,22 +28,28 @@ def _check_block(x: torch.Tensor, m: int, name: str) -> None:
 
 
 class GpuPlan:
-    def __init__(self, node_or_cptr, stream=None):
+    def __init__(self, node_or_cptr, stream=None, _handle=None):
         lib = _native.lib()
         self._owned_c = None
-        if isinstance(node_or_cptr, (tree.Dense, tree.HNode)):
-            cptr = tree.to_c(node_or_cptr)
-            self._owned_c = cptr
+        if _handle is not None:
+            self._h = _handle
+            mm = ctypes.c_int()
+            lib.dplr_gpu_plan_info(self._h, ctypes.byref(mm), None, None, None)
+            self.m = mm.value
         else:
-            cptr = node_or_cptr
-        self.m = int(cptr.contents.size)
-        h = ctypes.c_void_p()
-        _native.check(lib.dplr_gpu_plan_create(self.m, cptr, _stream_ptr(stream), ctypes.byref(h)),
-                      "dplr_gpu_plan_create")
-        self._h = h
-        if self._owned_c is not None:
-            tree.free_c(self._owned_c)
-            self._owned_c = None
+            if isinstance(node_or_cptr, (tree.Dense, tree.HNode)):
+                cptr = tree.to_c(node_or_cptr)
+                self._owned_c = cptr
+            else:
+                cptr = node_or_cptr
+            self.m = int(cptr.contents.size)
+            h = ctypes.c_void_p()
+            _native.check(lib.dplr_gpu_plan_create(self.m, cptr, _stream_ptr(stream), ctypes.byref(h)),
+                          "dplr_gpu_plan_create")
+            self._h = h
+            if self._owned_c is not None:
+                tree.free_c(self._owned_c)
+                self._owned_c = None
         mm, nnz, lev, mr = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
         lib.dplr_gpu_plan_info(self._h, ctypes.byref(mm), ctypes.byref(nnz), ctypes.byref(lev),
                                ctypes.byref(mr))
@@ -55,6 +61,40 @@ class GpuPlan:
 
     RESIDUAL_SLICED = 1
     SOLVE_MIXED = 2
+
+    @classmethod
+    def batch(cls, trees: list, stream=None) -> "GpuPlan":
+        """One plan over many independent matrices (block diagonal): matrix i
+        occupies rows offsets()[i] : offsets()[i] + trees[i].size."""
+        lib = _native.lib()
+        cptrs = [tree.to_c(t) for t in trees]
+        try:
+            arr = (tree.PDPlrMtx * len(cptrs))(*cptrs)
+            ms = (ctypes.c_int * len(trees))(*[t.size for t in trees])
+            h = ctypes.c_void_p()
+            _native.check(lib.dplr_gpu_batch_create(len(trees), ms, arr, _stream_ptr(stream),
+                                                    ctypes.byref(h)), "dplr_gpu_batch_create")
+        finally:
+            for c in cptrs:
+                tree.free_c(c)
+        return cls(None, _handle=h)
+
+    def offsets(self) -> list[int]:
+        """First row of every matrix of a batch ([0] for a single matrix)."""
+        lib = _native.lib()
+        cnt = ctypes.c_int()
+        _native.check(lib.dplr_gpu_batch_offsets(self._h, ctypes.byref(cnt), None), "dplr_gpu_batch_offsets")
+        rows = (ctypes.c_int * cnt.value)()
+        _native.check(lib.dplr_gpu_batch_offsets(self._h, None, rows), "dplr_gpu_batch_offsets")
+        return list(rows)
+
+    def autotune(self, n: int, stream=None) -> dict:
+        """Pick the fastest panel chunk length and right-hand-side tile of the
+        FP64 apply for n right-hand sides (call before factor())."""
+        c, nb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _native.check(_native.lib().dplr_gpu_autotune(self._h, int(n), _stream_ptr(stream), ctypes.byref(c),
+                                                      ctypes.byref(nb), ctypes.byref(ms)), "dplr_gpu_autotune")
+        return {"chunk_rows": c.value, "nb_cap": nb.value, "apply_ms": ms.value}
 
     def prepare_mixed(self, slices: int = 6, stream=None) -> None:
         """Sliced factor copies (3 to 6 bf16 slices) for the low-precision inner solve."""
@@ -215,3 +255,40 @@ class GpuPlan:
         if rc != -5 or strict:
             _native.check(rc, "dplr_gpu_solve_refined")
         return out, res.value, its.value
+
+
+class GpuGraph:
+    """A captured CUDA graph of one apply ('A') or solve ('S') of a plan with
+    fixed tensors x (input) and y (output); launch() replays it."""
+
+    def __init__(self, plan: GpuPlan, op: str, x: torch.Tensor, y: torch.Tensor, trans: str = "N",
+                 stream=None):
+        _check_block(x, plan.m, "x")
+        _check_block(y, plan.m, "y")
+        if x.shape != y.shape:
+            raise ValueError("x and y must have the same shape")
+        self.plan, self.x, self.y = plan, x, y
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().dplr_gpu_graph_create(plan.handle, op.encode(), trans.encode(), x.shape[0],
+                                                          x.data_ptr(), plan.m, y.data_ptr(), plan.m,
+                                                          _stream_ptr(stream), ctypes.byref(h)),
+                      "dplr_gpu_graph_create")
+        self._h = h
+
+    @property
+    def kernels(self) -> int:
+        return int(_native.lib().dplr_gpu_graph_kernels(self._h))
+
+    def launch(self, stream=None) -> None:
+        _native.check(_native.lib().dplr_gpu_graph_launch(self._h, _stream_ptr(stream)), "dplr_gpu_graph_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _native.lib().dplr_gpu_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

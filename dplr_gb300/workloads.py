@@ -1,0 +1,202 @@
+"""Secondary benchmark workloads (selected by ``bench.py --workload``).
+
+* ``apply``: the FP64 product Y = A X (dplrgepmv / dplrgepdmm) on the 2D
+  Gaussian-kernel matrix of the solve benchmark, for 1, 16 and 256
+  right-hand sides; the 1-RHS product is HBM-bound, so it is reported as
+  algorithmic GB/s (8 nnz + 16 N bytes per right-hand side) against the
+  measured copy bandwidth.
+* ``batched``: 512 independent 1D exponential-kernel matrices, N = 64 2^L
+  log-uniform in [1024, 16384], length scale uniform in [0.05, 0.5],
+  leaf 64, ranks 1 to 4, 1 to 16 right-hand sides each, FP64; one step is
+  one replay of a captured CUDA graph that applies all matrices and one of
+  a graph that solves all of them, after the autotuner picked the launch
+  shapes.
+* ``adjoint``: N = 65536 sorted uniform 1D points, exponential kernel
+  length 0.1 + 1e-2 I, leaf 128, rank 16, FP64; one step evaluates
+  L = ||A^-1 b - t||^2 and its gradient with respect to b and every factor:
+  refactorisation (the factors change between steps of an optimisation),
+  solve, transposed solve, factor gradient.
+
+Each returns the JSON record of its line; the caller adds clocks.
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import _native, gen
+from .plan import GpuGraph, GpuPlan
+
+
+def _events():
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _peaks(root):
+    try:
+        p = json.load(open(os.path.join(root, "MEASURED_PEAKS.json")))
+        return float(p["hbm_gbs"]), "of measured"
+    except Exception:
+        return 6800.0, "of fallback"
+
+
+def apply_workload(plan: GpuPlan, n: int, steps: int, warmup: int, root: str) -> dict:
+    """FP64 apply bandwidth for 1, 16 and 256 right-hand sides; the record's
+    value is the 1-RHS case."""
+    stream = torch.cuda.current_stream()
+    hbm, src = _peaks(root)
+    rows = {}
+    for nrhs in (1, 16, 256):
+        g = torch.Generator(device="cuda").manual_seed(11)
+        X = torch.randn(nrhs, n, generator=g, dtype=torch.float64, device="cuda")
+        Y = torch.empty_like(X)
+        for _ in range(max(3, warmup)):
+            plan.apply(X, out=Y)
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record(stream)
+        for _ in range(steps):
+            plan.apply(X, out=Y)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        by = 8.0 * plan.nnz + 16.0 * n * nrhs
+        fl = 2.0 * plan.nnz * nrhs
+        rows[nrhs] = {"ms": ms, "gbs": by / (ms / 1e3) / 1e9, "tflops": fl / (ms / 1e3) / 1e12,
+                      "frac_hbm": by / (ms / 1e3) / 1e9 / hbm, "frac_fp64": fl / (ms / 1e3) / 1e12 / 1.19}
+    one = rows[1]
+    return {
+        "metric": "FP64 PLR apply GB/s (1 RHS) @N=2^18", "value": one["gbs"], "unit": "GB/s",
+        "ms_per_step": one["ms"], "higher_is_better": True, "dtype": "f64",
+        "roofline": {"kernel": "apply (panel+reduce+expand)", "bound": "hbm", "achieved": one["gbs"],
+                     "peak": hbm, "unit": "GB/s", "frac": one["frac_hbm"], "traffic": None,
+                     "peak_source": src},
+        "by_rhs": rows,
+        "config": {"workload": f"FP64 apply of the 2D Gaussian-kernel PLR, N={n}, nnz={plan.nnz}",
+                   "bytes_per_rhs": "8*nnz + 16*N (factors read once, x read and y written once)"},
+    }
+
+
+def batched_trees(count: int = 512, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    trees, nrhs = [], []
+    for i in range(count):
+        L = int(rng.integers(4, 9))                   # N = 64 * 2^L in [1024, 16384]
+        n = 64 << L
+        x = np.sort(rng.uniform(0.0, 1.0, n))
+        trees.append(gen.exp1d_tree(x, ell=float(rng.uniform(0.05, 0.5)), shift=1e-2, leaf=64,
+                                    rank=int(rng.integers(1, 5)), seed=seed * 100000 + i))
+        nrhs.append(int(rng.integers(1, 17)))
+    return trees, nrhs
+
+
+def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
+    t0 = time.time()
+    trees, nrhs = batched_trees(count)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    plan = GpuPlan.batch(trees)
+    t_up = time.time() - t0
+    n = max(nrhs)
+    tune = plan.autotune(n)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    plan.factor()
+    torch.cuda.synchronize()
+    t_fac = time.time() - t0
+    offs = plan.offsets()
+    X = torch.zeros(n, plan.m, dtype=torch.float64, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(5)
+    for o, t, k in zip(offs, trees, nrhs):     # matrix i uses its first nrhs_i columns
+        X[:k, o:o + t.size] = torch.randn(k, t.size, generator=g, dtype=torch.float64, device="cuda")
+    Y = torch.empty_like(X)
+    Z = torch.empty_like(X)
+    ga = GpuGraph(plan, "A", X, Y)
+    gs = GpuGraph(plan, "S", X, Z)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, warmup)):
+        ga.launch()
+        gs.launch()
+    torch.cuda.synchronize()
+    l0 = _native.launch_count()
+    e0, e1 = _events()
+    e0.record(stream)
+    for _ in range(steps):
+        ga.launch()
+        gs.launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = _native.launch_count() - l0
+    ms = e0.elapsed_time(e1) / steps
+    # correctness of the replayed solve: residual of every matrix's columns
+    R = plan.residual(Z, X, precise=False)
+    rel = float((R.norm(dim=1) / X.norm(dim=1).clamp_min(1e-300)).max())
+    total_rhs = sum(nrhs)
+    return {
+        "metric": "batched PLR apply+solve RHS/s (512 matrices, uneven N/rank/RHS, graph replay)",
+        "value": 2.0 * total_rhs / (ms / 1e3), "unit": "RHS/s", "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f64", "gpu_launches": launches,
+        "config": {"workload": "512 1D exponential-kernel PLR matrices, N in [1024, 16384], leaf 64, "
+                               "ranks 1-4, 1-16 RHS each; one apply graph + one solve graph per step",
+                   "matrices": count, "rows_total": plan.m, "rhs_total": total_rhs, "rhs_stacked": n,
+                   "graph_kernels": {"apply": ga.kernels, "solve": gs.kernels},
+                   "autotune": tune, "unrefined_solve_rel_resid": rel,
+                   "setup_s": {"generate": t_gen, "upload": t_up, "factor": t_fac}},
+    }
+
+
+def adjoint_workload(steps: int, warmup: int, n: int = 65536) -> dict:
+    from .autograd import plr_solve
+    rng = np.random.default_rng(0)
+    x = np.sort(rng.uniform(0.0, 1.0, n))
+    t = gen.exp1d_tree(x, ell=0.1, shift=1e-2, leaf=128, rank=16, seed=1)
+    plan = GpuPlan(t)
+    pool = plan.read_pool()
+    b = torch.tensor(rng.standard_normal((1, n)), device="cuda")
+    tt = torch.tensor(rng.standard_normal((1, n)), device="cuda")
+
+    def step():
+        p = pool.clone().requires_grad_()     # new factor values: refactorised inside
+        bb = b.clone().requires_grad_()
+        xs = plr_solve(plan, p, bb)
+        loss = ((xs - tt) ** 2).sum()
+        loss.backward()
+        return loss, p.grad, bb.grad
+
+    for _ in range(max(3, warmup)):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    l0 = _native.launch_count()
+    e0, e1 = _events()
+    e0.record(stream)
+    for _ in range(steps):
+        loss, gp, gb = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # spot check against central differences (h = 1e-6) on two factor entries
+    blocks = plan.pool_blocks()
+    idx = [blocks[0]["u"] + 7, blocks[len(blocks) // 2]["d"] if "d" in blocks[len(blocks) // 2]
+           else blocks[len(blocks) // 2]["v"] + 3]
+    fd = []
+    with torch.no_grad():
+        for i in idx:
+            pp, pm = pool.clone(), pool.clone()
+            pp[i] += 1e-6
+            pm[i] -= 1e-6
+            lp = float(((plr_solve(plan, pp, b) - tt) ** 2).sum())
+            lm = float(((plr_solve(plan, pm, b) - tt) ** 2).sum())
+            fd.append({"index": i, "fd": (lp - lm) / 2e-6, "grad": float(gp[i])})
+    return {
+        "metric": "adjoint steps/s: loss=||A^-1 b - t||^2 and gradients (b, U, V, sig, leaves) @N=65536",
+        "value": 1000.0 / ms, "unit": "steps/s", "ms_per_step": ms, "higher_is_better": True,
+        "dtype": "f64", "gpu_launches": _native.launch_count() - l0,
+        "config": {"workload": "1D exponential kernel, N=65536, leaf 128, rank 16; factorisation, solve, "
+                               "transposed solve and factor gradient per step",
+                   "pool_doubles": plan.pool_size(), "loss": float(loss), "fd_check": fd},
+    }

@@ -38,6 +38,7 @@ extern "C" {
 #define DPLR_GPU_ESTATE     -6   /* plan not factored / wrong state */
 
 typedef struct dplr_gpu_plan_s *dplr_gpu_plan;
+typedef struct dplr_gpu_graph_s *dplr_gpu_graph;
 
 /* Thread-local description of the last failure ("" if none). */
 DPLR_API const char *dplr_gpu_last_error(void);
@@ -155,6 +156,39 @@ DPLR_API int dplr_gpu_pool_write(dplr_gpu_plan plan, const double *src, void *st
  * arrays.  No counterpart in DPLR. */
 DPLR_API int dplr_gpu_grad_factors(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *DY,
                                    int ldy, double alpha, double *G, void *stream);
+
+/* Batch of independent matrices as one plan: matrix i (size m[i], any
+ * depth and ranks) is the diagonal block of rows [off_i, off_i + m[i]) of
+ * one block-diagonal matrix, off_i = m[0] + ... + m[i-1]
+ * (dplr_gpu_batch_offsets).  Every plan function (apply, factor, solve,
+ * refined solve, gradients, pool access) then treats all matrices in the
+ * same kernel launches.  Right-hand sides are stacked the same way; a
+ * matrix with fewer right-hand sides than n leaves the extra columns
+ * unused.  No counterpart in DPLR, which handles one matrix per call.
+ * dplr_gpu_plan_refresh does not apply to batches (use dplr_gpu_pool_write). */
+DPLR_API int dplr_gpu_batch_create(int count, const int *m, DPlrMtx *const *A, void *stream,
+                                   dplr_gpu_plan *plan);
+DPLR_API int dplr_gpu_batch_offsets(dplr_gpu_plan plan, int *count, int *row0);
+
+/* CUDA graph of one apply (op 'A': Y = op(A) X) or one solve (op 'S':
+ * Y = op(A)^-1 X, needs dplr_gpu_factor) with fixed device arrays: built
+ * once (one ordinary run sizes the scratch, a second run is captured on an
+ * internal stream), then replayed by dplr_gpu_graph_launch on any stream
+ * with one launch call.  Valid while the plan, its factorisation and the
+ * arrays live; rebuild it after dplr_gpu_factor or dplr_gpu_autotune. */
+DPLR_API int dplr_gpu_graph_create(dplr_gpu_plan plan, char op, char trans, int n, const double *X,
+                                   int ldx, double *Y, int ldy, void *stream, dplr_gpu_graph *graph);
+DPLR_API int dplr_gpu_graph_launch(dplr_gpu_graph graph, void *stream);
+DPLR_API long long dplr_gpu_graph_kernels(dplr_gpu_graph graph);
+DPLR_API void dplr_gpu_graph_destroy(dplr_gpu_graph graph);
+
+/* Launch-shape autotuner of the FP64 kernels: times the apply with n
+ * right-hand sides for every panel chunk length (256 to 2048 rows) and
+ * right-hand-side tile (1 to 16 columns) and keeps the fastest in the plan.
+ * Call it before dplr_gpu_factor for the solve sweeps to use the tuned
+ * chunk length. */
+DPLR_API int dplr_gpu_autotune(dplr_gpu_plan plan, int n, void *stream, int *chunk_rows, int *nb_cap,
+                               double *best_ms);
 
 /* Instrumentation.  dplr_gpu_launch_count: kernels launched by this
  * library since load.  Between dplr_gpu_profile_start() and
