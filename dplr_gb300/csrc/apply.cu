@@ -88,6 +88,96 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
     }
 }
 
+// ------------------------------------------------------- one right-hand side
+// With a single right-hand side the apply is a pair of matrix-vector products
+// that stream every factor once: HBM- (and on GB300 FP64-FMA-) bound.  These
+// kernels read the factors straight from global memory with 16-byte loads,
+// several columns in flight per warp, and keep only x in shared memory.
+
+constexpr int kPanel1MaxLen = 2048;
+
+// Panel, 1 RHS: P[k] = F[r0:r0+len, k]^T x[in0+r0 : ...]; warp w handles
+// columns k = w, w+8, ... four at a time; shuffle reduction per column.
+__global__ void __launch_bounds__(kThreads) panel1_kernel(const PanelItem *__restrict__ items,
+                                                          const double *__restrict__ fbase,
+                                                          const double *__restrict__ X,
+                                                          double *__restrict__ partials)
+{
+    __shared__ __align__(16) double xs[kPanel1MaxLen];
+    const PanelItem it = items[blockIdx.x];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int r = t; r < it.len; r += kThreads) xs[r] = X[it.in0 + it.r0 + r];
+    __syncthreads();
+    const double *F = fbase + it.f + it.r0;
+    double *P = partials + it.p + (long long)it.chunk * it.rank;
+    const bool vec = ((it.n | it.r0 | it.len) & 1) == 0;
+    for (int k0 = warp; k0 < it.rank; k0 += 4 * (kThreads / 32)) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        if (vec) {
+            for (int r = 2 * lane; r < it.len; r += 64) {
+                const double2 xv = *reinterpret_cast<const double2 *>(xs + r);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int k = k0 + c * (kThreads / 32);
+                    if (k < it.rank) {
+                        const double2 fv = __ldg(reinterpret_cast<const double2 *>(F + (long long)k * it.n + r));
+                        acc[c] = fma(fv.x, xv.x, fma(fv.y, xv.y, acc[c]));
+                    }
+                }
+            }
+        } else {
+            for (int r = lane; r < it.len; r += 32) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int k = k0 + c * (kThreads / 32);
+                    if (k < it.rank) acc[c] = fma(__ldg(F + (long long)k * it.n + r), xs[r], acc[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            double v = acc[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            const int k = k0 + c * (kThreads / 32);
+            if (lane == 0 && k < it.rank) P[k] = v;
+        }
+    }
+}
+
+// Expand, 1 RHS, column-major terms only: y[tile] = alpha * sum_terms
+// A[tile, 0:K] b + beta y.  Thread (i, g) owns row i of the tile and the
+// inner indices k == g (mod G); the G partial sums meet in shared memory.
+__global__ void __launch_bounds__(kThreads) expand1_kernel(
+    const double *__restrict__ abase, const TileTerm *__restrict__ terms, const int *__restrict__ tile_row0,
+    const int *__restrict__ tile_begin, const double *__restrict__ T, const double *__restrict__ X,
+    double *__restrict__ Y, int R, double alpha, double beta)
+{
+    __shared__ double red[kThreads];
+    const int tile = blockIdx.x, row0 = tile_row0[tile];
+    const int t = threadIdx.x, G = kThreads / R, i = t % R, g = t / R;
+    double acc = 0.0, acc2 = 0.0;
+    for (int q = tile_begin[tile]; q < tile_begin[tile + 1]; ++q) {
+        const TileTerm tt = terms[q];
+        const double *A = abase + tt.a + i;
+        const double *B = tt.src == 0 ? T + tt.b : tt.src == 2 ? T + tt.b : X + tt.x_row0;
+        int k = g;
+        for (; k + G < tt.K; k += 2 * G) {
+            acc = fma(__ldg(A + (long long)k * tt.lda), __ldg(B + k), acc);
+            acc2 = fma(__ldg(A + (long long)(k + G) * tt.lda), __ldg(B + k + G), acc2);
+        }
+        if (k < tt.K) acc = fma(__ldg(A + (long long)k * tt.lda), __ldg(B + k), acc);
+    }
+    red[t] = acc + acc2;
+    __syncthreads();
+    if (t < R) {
+        double s = 0.0;
+        for (int gg = 0; gg < G; ++gg) s += red[gg * R + t];
+        double *y = Y + row0 + t;
+        *y = beta == 0.0 ? alpha * s : fma(alpha, s, beta * *y);
+    }
+}
+
 // ---------------------------------------------------------------- reduce
 // T[k, j] = sig[k] * sum_c P[c][k, j] (no scaling with a null sigbase);
 // grid.x = reduce item.
@@ -333,6 +423,12 @@ int run_panel(const Schedule &S, const double *fbase, const double *X, int ldx, 
         by += 8.0 * ((double)it.len * it.rank + (double)it.len * nrhs + (double)it.rank * nrhs);
     }
     ProfScope ps("panel", st, fl, by);
+    if (nrhs == 1 && S.max_len <= kPanel1MaxLen) {
+        panel1_kernel<<<(unsigned)S.items.size(), kThreads, 0, st>>>(S.d_items, fbase, X, partials);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
     DG_DISPATCH_NB(nb, (panel_kernel<NB><<<g, kThreads, 0, st>>>(S.d_items, fbase, X, ldx, nrhs,
                                                                   partials)));
     note_launch();
@@ -372,6 +468,12 @@ int run_expand(const Schedule &S, const double *abase, const double *T, const do
     }
     ProfScope ps("expand", st, fl, by);
     note_launch();
+    if (nrhs == 1 && !S.has_row_major) {
+        expand1_kernel<<<ntiles, kThreads, 0, st>>>(abase, S.d_terms, S.d_tile_row0, S.d_tile_begin, T, X, Y,
+                                                    S.tile_rows, alpha, beta);
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
     DG_DISPATCH_NB(nb, (expand_kernel<NB><<<g, kThreads, 0, st>>>(
                            abase, S.d_terms, S.d_tile_row0, S.d_tile_begin, T, X, ldx, Y, ldy,
                            nrhs, S.tile_rows, alpha, beta)));

@@ -119,6 +119,8 @@ struct Schedule {
     int tile_rows = 0;
     int max_rank = 0;
     int nb_cap = 16;                  // largest right-hand-side tile (autotuned)
+    int max_len = 0;                  // longest panel item (rows)
+    bool has_row_major = false;       // some term reads A row-major (trans_a)
     PanelItem *d_items = nullptr;
     ReduceItem *d_reduces = nullptr;
     int *d_tile_row0 = nullptr, *d_tile_begin = nullptr;

@@ -257,6 +257,10 @@ static int upload_vec(const std::vector<T> &v, T **dst, long long *bytes)
 
 int upload_schedule(Schedule &S, long long *bytes)
 {
+    S.max_len = 0;
+    for (const PanelItem &it : S.items) S.max_len = std::max(S.max_len, it.len);
+    S.has_row_major = false;
+    for (const TileTerm &t : S.terms) S.has_row_major = S.has_row_major || t.trans_a;
     int rc;
     if ((rc = upload_vec(S.items, &S.d_items, bytes))) return rc;
     if ((rc = upload_vec(S.reduces, &S.d_reduces, bytes))) return rc;

@@ -610,8 +610,11 @@ static void launch_panel(const Plan *p, const SSchedule &S, const bf16 *apool, l
     if (S.tile_m == tc::M) {
         const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
         const unsigned kt = (unsigned)((S.max_rank + tc::M - 1) / tc::M);
-        tc::tc_panel_kernel<NS, D><<<dim3((unsigned)S.items.size(), rt, kt), tc::THREADS, tc::Cfg<NS>::SMEM, st>>>(
-            S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials, p->tc_err_d);
+        const unsigned ni = (unsigned)S.items.size();
+        const int on_x = ni > 65535u;
+        tc::tc_panel_kernel<NS, D><<<on_x ? dim3(ni, rt, kt) : dim3(rt, ni, kt), tc::THREADS, tc::Cfg<NS>::SMEM,
+                                     st>>>(S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials, p->tc_err_d,
+                                           on_x);
     } else {
         const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
         sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rt), kSThreads,
@@ -631,9 +634,11 @@ static void launch_expand(const Plan *p, const SSchedule &S, const bf16 *apool, 
     const unsigned ntiles = (unsigned)S.tile_row0.size();
     if (S.tile_m == tc::M) {
         const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
-        tc::tc_expand_kernel<NS, D><<<dim3(ntiles, rt), tc::THREADS, tc::Cfg<NS>::SMEM, st>>>(
+        const int on_x = ntiles > 65535u;
+        tc::tc_expand_kernel<NS, D><<<on_x ? dim3(ntiles, rt) : dim3(rt, ntiles), tc::THREADS, tc::Cfg<NS>::SMEM,
+                                      st>>>(
             S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
-            xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+            xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d, on_x);
     } else {
         const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
         sp_expand_kernel<NS, NS, D><<<dim3(ntiles, rt), kSThreads, (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(

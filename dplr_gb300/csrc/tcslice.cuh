@@ -234,29 +234,33 @@ __device__ __forceinline__ void drain(Ctl &c, int last_block)
 template <int D>
 __device__ __forceinline__ void read_group(uint32_t trow, int c8, __int128 (&W)[8])
 {
+    constexpr int DH = D >= 6 ? D - 4 : 1;       // diagonals 2..DH go to ghi (none when DH < 2)
     long long ghi[8], glo[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) ghi[u] = glo[u] = 0;
-    if (D >= 6) {
+    if (DH >= 2) {
+        uint32_t r[DH >= 2 ? DH - 1 : 1][8];
 #pragma unroll
-        for (int d = 2; d <= (D >= 6 ? D - 4 : 2); ++d) {
-            uint32_t r[8];
-            ld8(trow + (uint32_t)((d - 2) * N + c8 * 8), r);
-            ld_wait();
-#pragma unroll
-            for (int u = 0; u < 8; ++u) ghi[u] += fint(r[u], 7 * (D - 4 - d));
-        }
-    }
-#pragma unroll
-    for (int d = (D >= 6 ? D - 3 : 2); d <= D; ++d) {
-        uint32_t r[8];
-        ld8(trow + (uint32_t)((d - 2) * N + c8 * 8), r);
+        for (int d = 2; d <= DH; ++d) ld8(trow + (uint32_t)((d - 2) * N + c8 * 8), r[d - 2]);
         ld_wait();
 #pragma unroll
-        for (int u = 0; u < 8; ++u) glo[u] += fint(r[u], 7 * (D - d));
+        for (int d = 2; d <= DH; ++d)
+#pragma unroll
+            for (int u = 0; u < 8; ++u) ghi[u] += fint(r[d - 2][u], 7 * (D - 4 - d));
+    }
+    {
+        constexpr int D0 = DH + 1;
+        uint32_t r[D - D0 + 1][8];
+#pragma unroll
+        for (int d = D0; d <= D; ++d) ld8(trow + (uint32_t)((d - 2) * N + c8 * 8), r[d - D0]);
+        ld_wait();
+#pragma unroll
+        for (int d = D0; d <= D; ++d)
+#pragma unroll
+            for (int u = 0; u < 8; ++u) glo[u] += fint(r[d - D0][u], 7 * (D - d));
     }
 #pragma unroll
-    for (int u = 0; u < 8; ++u) W[u] = (D >= 6 ? ((__int128)ghi[u] << 28) : (__int128)0) + glo[u];
+    for (int u = 0; u < 8; ++u) W[u] = (DH >= 2 ? ((__int128)ghi[u] << 28) : (__int128)0) + glo[u];
 }
 
 // ------------------------------------------------------------- panel
@@ -266,14 +270,16 @@ template <int NS, int D>
 __global__ void __launch_bounds__(THREADS, 1)
     tc_panel_kernel(const SPanelItem *__restrict__ items, const bf16 *__restrict__ apool, long long astride,
                     const bf16 *__restrict__ xs, long long xstride, int ldx, int nrhs,
-                    __int128 *__restrict__ partials, int *err)
+                    __int128 *__restrict__ partials, int *err, int items_on_x)
 {
     using C = Cfg<NS>;
     constexpr int TC = tmem_cols(D);
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ Ctl ctl;
-    const SPanelItem it = items[blockIdx.x];
-    const int j0 = blockIdx.y * N;
+    // right-hand-side tiles of one item run side by side (grid.x) unless
+    // the item count exceeds grid.y's range
+    const SPanelItem it = items[items_on_x ? blockIdx.x : blockIdx.y];
+    const int j0 = (items_on_x ? blockIdx.y : blockIdx.x) * N;
     const int kt = blockIdx.z * M;          // rank tile
     if (kt >= it.rank) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -395,17 +401,19 @@ __global__ void __launch_bounds__(THREADS, 1)
                      const int *__restrict__ aexp, const bf16 *__restrict__ ts, long long tstride,
                      const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int ldx,
                      const int *__restrict__ xexp, int nrhs, int neg, const double *__restrict__ Bin,
-                     int ldbin, int addb, double *__restrict__ Y, int ldy, int *err)
+                     int ldbin, int addb, double *__restrict__ Y, int ldy, int *err, int tiles_on_x)
 {
     using C = Cfg<NS>;
     constexpr int TC = tmem_cols(D);
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ Ctl ctl;
     __shared__ int cmax[N];
-    const int tile = blockIdx.x;
+    // right-hand-side tiles of one row tile run side by side (grid.x) unless
+    // the tile count exceeds grid.y's range
+    const int tile = tiles_on_x ? blockIdx.x : blockIdx.y;
     const int row0 = tile_row0[tile];
     const int q0 = tile_begin[tile], q1 = tile_begin[tile + 1];
-    const int j0 = blockIdx.y * N;
+    const int j0 = (tiles_on_x ? blockIdx.y : blockIdx.x) * N;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int lq = warp & 3, ch = warp >> 2;
     const int row = lq * 32 + lane;
