@@ -16,13 +16,25 @@
 #include "sliced.cuh"
 #include "factor.cuh"
 #include "tcslice.cuh"
+#include "tcpipe.cuh"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
 
 namespace dg {
+
+struct Fact;
+static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st);
+static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int ldx, const double *B, int ldb,
+                              double *R, int ldr, cudaStream_t st);
+template <int NS>
+static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st);
+template <int NS>
+static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const double *B, int ldb, double *X, int ldx,
+                          cudaStream_t st);
 
 constexpr int SK = 64;          // inner-dimension rows per stage
 constexpr int SLD = SK + 8;     // padded smem row (bf16 elements)
@@ -562,7 +574,8 @@ static long long al32(long long x) { return (x + 31) & ~31LL; }
 static int pad8(int x) { return (x + 7) & ~7; }
 
 // Expand tile height: 128 rows on the tcgen05 kernels when every leaf is a
-// multiple of 128 rows, else 64 rows on the mma.sync kernels.
+// multiple of 128 rows and no rank exceeds 256, else 64 rows on the
+// mma.sync kernels.
 // DPLR_GB300_SLICED_MMA=1 selects the mma.sync kernels everywhere.
 static int sliced_tile_rows(const Plan *p)
 {
@@ -570,6 +583,7 @@ static int sliced_tile_rows(const Plan *p)
     if (env && env[0] == '1') return ST;
     for (const LeafDesc &L : p->leaves)
         if (L.b % tc::M != 0 || L.row0 % tc::M != 0) return ST;
+    if (p->max_rank > 256) return ST;         // the tile-block layouts hold at most 4 rank tiles of 64
     return tc::M;
 }
 
@@ -659,6 +673,10 @@ static int dev_vec(const std::vector<T> &v, T **dst, long long *bytes)
 
 static void free_sschedule(SSchedule &A)
 {
+    cudaFree(A.d_pitems);
+    cudaFree(A.d_xterms);
+    A.d_pitems = nullptr;
+    A.d_xterms = nullptr;
     cudaFree(A.d_items);
     cudaFree(A.d_reduces);
     cudaFree(A.d_tile_row0);
@@ -706,6 +724,7 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
     Sliced *S = new Sliced();
     p->sliced = S;
     S->ns = ns;
+    if (sliced_tile_rows(p) == tc::M) return sliced_build_tb(p, S, st);
 
     // layout: V column-major (ld n), U row-major (stride pad8(rank)), leaves row-major
     std::vector<long long> vs_off(p->lr.size()), us_off(p->lr.size()), ds_off(p->leaves.size());
@@ -920,6 +939,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
     Sliced *S = (Sliced *)p->sliced;
     if (!S) return fail(DPLR_GPU_ESTATE, "sliced residual: plan has no sliced factors");
     if (nrhs <= 0 || p->m == 0) return 0;
+    if (S->apply.tile_m == tc::M) return sliced_residual_tb(p, S, nrhs, X, ldx, B, ldb, R, ldr, st);
     const int m = p->m;
     const SSchedule &A = S->apply;
     SWork w;
@@ -1075,6 +1095,14 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
     MixedSliced *M = new MixedSliced();
     p->mixed = M;
     M->ns = ns;
+    if (sliced_tile_rows(p) == tc::M) {
+        switch (ns) {
+        case 3: return mixed_build_tb_t<3>(p, M, F, st);
+        case 4: return mixed_build_tb_t<4>(p, M, F, st);
+        case 5: return mixed_build_tb_t<5>(p, M, F, st);
+        default: return mixed_build_tb_t<6>(p, M, F, st);
+        }
+    }
     const int m = p->m;
     const int nlev = (int)F->lv.size();
 
@@ -1344,6 +1372,14 @@ int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx,
     Fact *F = (Fact *)p->fact;
     if (!M || !F) return fail(DPLR_GPU_ESTATE, "mixed solve: not prepared");
     if (nrhs <= 0 || p->m == 0) return 0;
+    if (M->leaf.tile_m == tc::M) {
+        switch (M->ns) {
+        case 3: return mixed_solve_tb<3>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        case 4: return mixed_solve_tb<4>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        case 5: return mixed_solve_tb<5>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        default: return mixed_solve_tb<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        }
+    }
     switch (M->ns) {
     case 3: return mixed_solve_t<3>(p, M, F, nrhs, B, ldb, X, ldx, st);
     case 4: return mixed_solve_t<4>(p, M, F, nrhs, B, ldb, X, ldx, st);
@@ -1351,5 +1387,776 @@ int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx,
     default: return mixed_solve_t<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
     }
 }
+
+
+// ====================================================== tcgen05 pipeline path
+//
+// With every leaf a multiple of 128 rows the products run on the
+// warp-specialised tcgen05 kernels of tcpipe.cuh.  Their operands are cut
+// into tile-blocks (R rows x 16 inner elements, contiguous, in the tensor
+// core's K-major core-matrix order), so that one pipeline stage is a few
+// contiguous bulk copies:
+//   V (panel, B operand)   per block and rank tile of <= 64: row-blocks of 16
+//                          block rows, pad16(tile ranks) rows each;
+//   U, leaves, Z_l, leaf inverses (expand, A operand): 128-row tiles x
+//                          16-element blocks of the inner dimension;
+//   X slices (panel A operand in pairs, leaf-term B operand): 16-row blocks
+//                          x 64-column tiles (column count padded to 128);
+//   T / W slices (expand B operand): per block, 64-column tiles x 16-rank
+//                          blocks.
+// Padding rows and columns are zero.
+
+namespace {
+
+constexpr int kTbA = tc2::TB_A;     // 128 x 16
+constexpr int kTbB = tc2::TB_B;     // 64 x 16
+
+int pad16(int x) { return (x + 15) & ~15; }
+
+// V into tile-blocks: one CTA per (job, rank column).
+struct VSliceJob {
+    long long src;          // column-major n x rank (ld n)
+    long long dst[4];       // tile-block base of rank tiles 0..3
+    int nr[4];              // padded rows of those tiles
+    int n, rank, exp;
+};
+
+template <int NS>
+__global__ void slice_v_tb_kernel(const VSliceJob *jobs, const int *col_base, int njobs, const double *src,
+                                  bf16 *dst, long long stride, int *exps)
+{
+    __shared__ double red[256];
+    const int gc = blockIdx.x;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (col_base[mid] <= gc) lo = mid; else hi = mid - 1;
+    }
+    const VSliceJob &J = jobs[lo];
+    const int k = gc - col_base[lo];
+    const double *col = src + J.src + (long long)k * J.n;
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) mx = fmax(mx, fabs(col[i]));
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const int e = scale_exp(red[0]);
+    if (threadIdx.x == 0) exps[J.exp + k] = e;
+    const int kt = k / 64, r = k % 64, nr = J.nr[kt];
+    bf16 *base = dst + J.dst[kt];
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x)
+        slice_d<NS>(col[i], e, base + (long long)(i >> 4) * nr * 16 + tc2::tbo(r, i & 15), stride);
+}
+
+// Row-sliced operands into 128-row tile-blocks: one thread per row.
+struct RSliceJob {
+    long long src;          // column-major rows x cols (ld)
+    long long dst;          // tile-block base
+    int ld, rows, cols, nkb, exp;
+};
+
+template <int NS>
+__global__ void slice_r_tb_kernel(const RSliceJob *jobs, const int *row_base, int njobs, int total, const double *src,
+                                  bf16 *dst, long long stride, int *exps)
+{
+    const int gr = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gr >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (row_base[mid] <= gr) lo = mid; else hi = mid - 1;
+    }
+    const RSliceJob &J = jobs[lo];
+    const int r = gr - row_base[lo];
+    double mx = 0.0;
+    for (int k = 0; k < J.cols; ++k) mx = fmax(mx, fabs(src[J.src + r + (long long)k * J.ld]));
+    const int e = scale_exp(mx);
+    exps[J.exp + r] = e;
+    bf16 *base = dst + J.dst + (long long)(r >> 7) * J.nkb * kTbA;
+    for (int k = 0; k < J.nkb * 16; ++k) {
+        const double v = k < J.cols ? src[J.src + r + (long long)k * J.ld] : 0.0;
+        slice_d<NS>(v, e, base + (long long)(k >> 4) * kTbA + tc2::tbo(r & 127, k & 15), stride);
+    }
+}
+
+// Pack the NS slices of 8 consecutive values into one 16-byte store per slice.
+template <int NS>
+__device__ __forceinline__ void store8(const long long (&y)[8], bf16 *out, long long stride)
+{
+    int a[8][NS];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        long long v = y[u];
+#pragma unroll
+        for (int p = NS - 1; p >= 1; --p) {
+            const long long d = ((v + 64) & 127) - 64;
+            a[u][p] = (int)d;
+            v = (v - d) >> 7;
+        }
+        a[u][0] = (int)v;
+    }
+#pragma unroll
+    for (int p = 0; p < NS; ++p) {
+        uint4 w;
+        uint32_t h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint16_t lo16 = __bfloat16_as_ushort(__float2bfloat16_rn((float)a[2 * q][p]));
+            const uint16_t hi16 = __bfloat16_as_ushort(__float2bfloat16_rn((float)a[2 * q + 1][p]));
+            h[q] = (uint32_t)lo16 | ((uint32_t)hi16 << 16);
+        }
+        w.x = h[0];
+        w.y = h[1];
+        w.z = h[2];
+        w.w = h[3];
+        *reinterpret_cast<uint4 *>(out + p * stride) = w;
+    }
+}
+
+// X (m x nrhs) into 16-row x 64-column tile-blocks; one thread per
+// (column j, row-block rb), j fastest; columns >= nrhs are zero.
+template <int NS>
+__global__ void xslice_tb_kernel(const double *X, int m, int ldx, int nrhs, int xnjt, const int *xexp, bf16 *xs,
+                                 long long stride)
+{
+    const int nrb = m >> 4, ncol = xnjt * 64;
+    const long long cnt = (long long)nrb * ncol;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(t % ncol), rb = (int)(t / ncol);
+        const bool live = j < nrhs;
+        const int sh = live ? 7 * NS - xexp[j] : 0;
+        const double *col = X + (long long)(live ? j : 0) * ldx + rb * 16;
+        bf16 *out = xs + ((long long)rb * xnjt + (j >> 6)) * kTbB + tc2::tbo(j & 63, 0);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            long long y[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) y[u] = live ? scaled_int(col[h * 8 + u], sh) : 0;
+            store8<NS>(y, out + h * 64, stride);
+        }
+    }
+}
+
+// T / W (rank x nrhs per block, FP64 or double-double) into tile-blocks of
+// 64 columns x 16 ranks; one warp per (block, column j < njt * 64).
+template <int NS>
+__global__ void tslice_tb_kernel(const SReduceItem *__restrict__ items, int nitems, const double *__restrict__ T,
+                                 long long lo_off, int nrhs, int njt, bf16 *__restrict__ ts, long long tstride,
+                                 int *__restrict__ texp)
+{
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int ncol = njt * 64;
+    if (w >= (long long)nitems * ncol) return;
+    const int b = (int)(w / ncol), j = (int)(w % ncol);
+    const SReduceItem R = items[b];
+    const bool live = j < nrhs;
+    const double *th = T + R.t * nrhs + (long long)(live ? j : 0) * R.rank;
+    const double *tl = lo_off >= 0 ? th + lo_off : nullptr;
+    double mx = 0.0;
+    if (live)
+        for (int k = lane; k < R.rank; k += 32) mx = fmax(mx, fabs(th[k]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = scale_exp(mx);
+    if (live && lane == 0) texp[(long long)b * nrhs + j] = e;
+    const int nkb = R.rp >> 4;
+    bf16 *base = ts + R.tpad * njt + (long long)(j >> 6) * nkb * kTbB;
+    for (int k = lane; k < nkb * 16; k += 32) {
+        bf16 *o = base + (long long)(k >> 4) * kTbB + tc2::tbo(j & 63, k & 15);
+        if (live && k < R.rank) {
+            slice_dd<NS>(th[k], tl ? tl[k] : 0.0, e, o, tstride);
+        } else {
+            const bf16 zero = __float2bfloat16(0.0f);
+#pragma unroll
+            for (int p = 0; p < NS; ++p) o[p * tstride] = zero;
+        }
+    }
+}
+
+int upload_tb(SSchedule &S, long long *bytes)
+{
+    int rc;
+    if ((rc = dev_vec(S.pitems, &S.d_pitems, bytes)) || (rc = dev_vec(S.reduces, &S.d_reduces, bytes)) ||
+        (rc = dev_vec(S.tile_row0, &S.d_tile_row0, bytes)) || (rc = dev_vec(S.tile_begin, &S.d_tile_begin, bytes)) ||
+        (rc = dev_vec(S.xterms, &S.d_xterms, bytes)))
+        return rc;
+    return 0;
+}
+
+// V tile-block layout of every low-rank block (shared by both builders).
+struct VLayout {
+    std::vector<VSliceJob> jobs;
+    std::vector<int> col_base;
+    int ncols = 0;
+};
+
+long long layout_v(const Plan *p, std::vector<std::array<long long, 4>> &vdst, std::vector<std::array<int, 4>> &vnr,
+                   long long el, const std::vector<int> &ev_off, VLayout &VL)
+{
+    vdst.assign(p->lr.size(), {0, 0, 0, 0});
+    vnr.assign(p->lr.size(), {0, 0, 0, 0});
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        VSliceJob J{};
+        J.src = L.v;
+        J.n = L.n;
+        J.rank = L.rank;
+        J.exp = ev_off[b];
+        for (int kt = 0; kt * 64 < L.rank; ++kt) {
+            const int nr = pad16(std::min(64, L.rank - kt * 64));
+            vdst[b][kt] = el;
+            vnr[b][kt] = nr;
+            J.dst[kt] = el;
+            J.nr[kt] = nr;
+            el += (long long)(L.n / 16) * nr * 16;
+        }
+        VL.col_base.push_back(VL.ncols);
+        VL.jobs.push_back(J);
+        VL.ncols += L.rank;
+    }
+    return el;
+}
+
+// Panel items of one block (row chunks of CH rows x rank tiles of 64).
+void panel_items(const LRDesc &L, const std::array<long long, 4> &vdst, const std::array<int, 4> &vnr, long long poff,
+                 std::vector<PItem> &out)
+{
+    const int CH = 1024;
+    const int nch = (L.n + CH - 1) / CH;
+    for (int c = 0; c < nch; ++c) {
+        const int r0 = c * CH, len = std::min(CH, L.n - r0);
+        for (int kt = 0; kt * 64 < L.rank; ++kt) {
+            PItem it;
+            it.v = vdst[kt];
+            it.p = poff;
+            it.rank = L.rank;
+            it.kt = kt * 64;
+            it.nr = vnr[kt];
+            it.xrb0 = (L.col0 + r0) / 16;
+            it.vrb0 = r0 / 16;
+            it.nkb = len / 16;
+            it.chunk = c;
+            out.push_back(it);
+        }
+    }
+}
+
+int xnjt_of(int nrhs) { return 2 * ((nrhs + 127) / 128); }
+
+// X slices (tile-blocks) and their exponents for nrhs columns.
+template <int NS>
+int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_elems, int *&xexp, size_t &xexp_n,
+               cudaStream_t st)
+{
+    const int xnjt = xnjt_of(nrhs);
+    const size_t need = (size_t)NS * (m / 16) * xnjt * kTbB;
+    if (xs_elems < need) {
+        cudaFree(xs);
+        xs = nullptr;
+        xs_elems = 0;
+        if (cudaMalloc((void **)&xs, need * sizeof(bf16)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate X slices");
+        xs_elems = need;
+    }
+    if (xexp_n < (size_t)nrhs) {
+        cudaFree(xexp);
+        xexp = nullptr;
+        if (cudaMalloc((void **)&xexp, nrhs * sizeof(int)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
+        xexp_n = nrhs;
+    }
+    xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, xexp);
+    note_launch();
+    const long long cnt = (long long)(m / 16) * xnjt * 64;
+    const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 16);
+    xslice_tb_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <int NS, int D>
+int tb_attrs()
+{
+    DG_CUDA(cudaFuncSetAttribute(tc2::panel_kernel<NS, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc2::Cfg<NS>::SMEM));
+    DG_CUDA(cudaFuncSetAttribute(tc2::expand_kernel<NS, D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc2::Cfg<NS>::SMEM));
+    if constexpr (D <= 7)
+        DG_CUDA(cudaFuncSetAttribute(tc2::expand_kernel<NS, D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     tc2::Cfg<NS>::SMEM));
+    return 0;
+}
+
+int grid_of(long long units)
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (int)std::max<long long>(1, std::min<long long>(units, sms));
+}
+
+template <int NS, int D>
+void launch_panel_tb(const Plan *p, const SSchedule &S, const bf16 *vpool, long long vstride, const bf16 *xs,
+                     int m, int nrhs, __int128 *partials, cudaStream_t st)
+{
+    const int njp = (nrhs + 127) / 128;
+    const int n = (int)S.pitems.size();
+    if (n == 0) return;
+    tc2::panel_kernel<NS, D><<<grid_of((long long)n * njp), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
+        S.d_pitems, n, njp, vpool, vstride, xs, (long long)(m / 16) * xnjt_of(nrhs) * kTbB, xnjt_of(nrhs), nrhs,
+        partials, p->tc_err_d);
+    note_launch();
+}
+
+template <int NS, int D>
+void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
+                      const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, int m, const int *xexp,
+                      int nrhs, bool neg, const double *Bin, int ldbin, bool addb, double *Y, int ldy,
+                      cudaStream_t st)
+{
+    const int njt = (nrhs + 63) / 64;
+    const int nt = (int)S.tile_row0.size();
+    if (nt == 0) return;
+    const long long xstride = (long long)(m / 16) * xnjt_of(nrhs) * kTbB;
+    bool single = true;                         // every tile one term: the 64-bit epilogue applies
+    for (size_t t = 0; t + 1 < S.tile_begin.size(); ++t) single = single && S.tile_begin[t + 1] - S.tile_begin[t] == 1;
+    if constexpr (D <= 7) {
+        if (single) {
+            tc2::expand_kernel<NS, D, true><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
+                S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs,
+                xstride, xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+            note_launch();
+            return;
+        }
+    }
+    tc2::expand_kernel<NS, D, false><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
+        S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs, xstride,
+        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+    note_launch();
+}
+
+}  // namespace
+
+// -------------------------------------------------- exact-slice residual
+static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
+{
+    std::vector<int> ev_off(p->lr.size()), eu_off(p->lr.size()), ed_off(p->leaves.size());
+    int nexp = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        ev_off[b] = nexp;
+        nexp += p->lr[b].rank;
+        eu_off[b] = nexp;
+        nexp += p->lr[b].n;
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        ed_off[i] = nexp;
+        nexp += p->leaves[i].b;
+    }
+    VLayout VL;
+    std::vector<std::array<long long, 4>> vdst;
+    std::vector<std::array<int, 4>> vnr;
+    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL);
+    std::vector<long long> ua(p->lr.size(), 0), la(p->leaves.size(), 0);
+    std::vector<RSliceJob> rj;
+    std::vector<int> rbase;
+    int nrows = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        const int nkb = (L.rank + 15) / 16;
+        ua[b] = el;
+        el += (long long)(L.n / tc2::M) * nkb * kTbA;
+        rbase.push_back(nrows);
+        rj.push_back(RSliceJob{L.u, ua[b], L.n, L.n, L.rank, nkb, eu_off[b]});
+        nrows += L.n;
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        la[i] = el;
+        el += (long long)(L.b / tc2::M) * (L.b / 16) * kTbA;
+        rbase.push_back(nrows);
+        rj.push_back(RSliceJob{L.d, la[i], L.b, L.b, L.b, L.b / 16, ed_off[i]});
+        nrows += L.b;
+    }
+    S->stride = al32(std::max<long long>(el, 1));
+    if (cudaMalloc((void **)&S->pool, (size_t)kNS * S->stride * sizeof(bf16)) != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate slices");
+    S->bytes += (long long)kNS * S->stride * 2;
+    DG_CUDA(cudaMemsetAsync(S->pool, 0, (size_t)kNS * S->stride * sizeof(bf16), st));
+    S->nexp = nexp;
+    int rc;
+    if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &S->exps, &S->bytes))) return rc;
+    {
+        VSliceJob *d_vj = nullptr;
+        RSliceJob *d_rj = nullptr;
+        int *d_vb = nullptr, *d_rb = nullptr;
+        long long tmp = 0;
+        if ((rc = dev_vec(VL.jobs, &d_vj, &tmp)) || (rc = dev_vec(VL.col_base, &d_vb, &tmp)) ||
+            (rc = dev_vec(rj, &d_rj, &tmp)) || (rc = dev_vec(rbase, &d_rb, &tmp)))
+            return rc;
+        if (VL.ncols > 0) {
+            slice_v_tb_kernel<kNS><<<VL.ncols, 256, 0, st>>>(d_vj, d_vb, (int)VL.jobs.size(), p->pool, S->pool,
+                                                            S->stride, S->exps);
+            note_launch();
+        }
+        if (nrows > 0) {
+            slice_r_tb_kernel<kNS><<<(nrows + 127) / 128, 128, 0, st>>>(d_rj, d_rb, (int)rj.size(), nrows, p->pool,
+                                                                       S->pool, S->stride, S->exps);
+            note_launch();
+        }
+        cudaError_t e2 = cudaGetLastError();
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+        cudaFree(d_vj);
+        cudaFree(d_vb);
+        cudaFree(d_rj);
+        cudaFree(d_rb);
+        if (e2 != cudaSuccess) return fail(DPLR_GPU_ECUDA, "slicing: %s", cudaGetErrorString(e2));
+    }
+    // schedule: panel items, reduces, 128-row tiles
+    SSchedule &A = S->apply;
+    A.tile_m = tc2::M;
+    long long poff = 0, tpre = 0;
+    std::vector<int> ridx(p->lr.size(), -1);
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        panel_items(L, vdst[b], vnr[b], poff, A.pitems);
+        const int nch = (L.n + 1023) / 1024;
+        const int nkb = (L.rank + 15) / 16;
+        ridx[b] = (int)A.reduces.size();
+        A.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], nkb * 16, tpre});
+        poff += (long long)nch * L.rank;
+        tpre += (long long)nkb * kTbB;
+        A.max_rank = std::max(A.max_rank, L.rank);
+    }
+    A.partial_per_rhs = poff;
+    A.t_per_rhs = p->total_rank;
+    A.tpre = tpre;
+    const int ntiles = p->m / tc2::M;
+    std::vector<std::vector<XTerm>> per(ntiles);
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0) continue;
+        const int nkb = (L.rank + 15) / 16;
+        for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += tc2::M)
+            per[t0 / tc2::M].push_back(XTerm{ua[b] + (long long)((t0 - L.row0) / tc2::M) * nkb * kTbA,
+                                             A.reduces[ridx[b]].tpad, L.rank, eu_off[b] + (t0 - L.row0), 0, ridx[b]});
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += tc2::M)
+            per[t0 / tc2::M].push_back(XTerm{la[i] + (long long)((t0 - L.row0) / tc2::M) * (L.b / 16) * kTbA,
+                                             L.row0 / 16, L.b, ed_off[i] + (t0 - L.row0), 1, -1});
+    }
+    for (int t = 0; t < ntiles; ++t) {
+        A.tile_row0.push_back(t * tc2::M);
+        A.tile_begin.push_back((int)A.xterms.size());
+        A.xterms.insert(A.xterms.end(), per[t].begin(), per[t].end());
+    }
+    A.tile_begin.push_back((int)A.xterms.size());
+    if ((rc = upload_tb(A, &S->bytes))) return rc;
+    if ((rc = ensure_err_flag(p))) return rc;
+    return tb_attrs<kNS, kD>();
+}
+
+static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int ldx, const double *B, int ldb,
+                              double *R, int ldr, cudaStream_t st)
+{
+    const int m = p->m;
+    const SSchedule &A = S->apply;
+    const int njt = (nrhs + 63) / 64;
+    int rc;
+    {
+        ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * kNS * m * nrhs);
+        if ((rc = slice_x_tb<kNS>(X, m, ldx, nrhs, S->xs, S->xs_elems, S->xexp, S->xexp_n, st))) return rc;
+    }
+    // scratch: partials, DD T, T slices, T exponents (256-byte carves)
+    auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t part_bytes = r256((size_t)A.partial_per_rhs * nrhs * sizeof(__int128));
+    const size_t t_bytes = r256((size_t)2 * A.t_per_rhs * nrhs * sizeof(double));
+    const long long tstride = A.tpre * njt;
+    const size_t ts_bytes = r256((size_t)kNS * tstride * sizeof(bf16));
+    const size_t te_bytes = r256((size_t)std::max<size_t>(A.reduces.size(), 1) * nrhs * sizeof(int));
+    const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes;
+    if (S->work_bytes < need) {
+        cudaFree(S->work);
+        S->work = nullptr;
+        S->work_bytes = 0;
+        if (cudaMalloc(&S->work, need) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate scratch");
+        S->work_bytes = need;
+    }
+    char *base = reinterpret_cast<char *>(S->work);
+    __int128 *partials = reinterpret_cast<__int128 *>(base);
+    double *T = reinterpret_cast<double *>(base + part_bytes);
+    const long long lo_off = A.t_per_rhs * nrhs;
+    bf16 *ts = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes);
+    int *texp = reinterpret_cast<int *>(base + part_bytes + t_bytes + ts_bytes);
+    int npairs = 0;
+    for (int d = 2; d <= kD; ++d)
+        for (int pp = std::max(1, d - kNS); pp <= std::min(kNS, d - 1); ++pp) ++npairs;
+    if (!A.pitems.empty()) {
+        double fl = 0, by = 0;
+        for (const PItem &it : A.pitems) {
+            fl += 2.0 * it.nkb * 16 * std::min(64, it.rank - it.kt) * nrhs;
+            by += 2.0 * kNS * ((double)it.nkb * 16 * it.nr + (double)it.nkb * 16 * nrhs);
+        }
+        {
+            ProfScope ps("sliced_panel", st, fl * npairs, by);
+            launch_panel_tb<kNS, kD>(p, A, S->pool, S->stride, S->xs, m, nrhs, partials, st);
+            DG_CUDA(cudaGetLastError());
+        }
+        ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
+        const long long maxcnt = (long long)A.max_rank * nrhs;
+        sp_reduce_kernel<kD><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+            A.d_reduces, partials, S->exps, S->xexp, p->pool, nrhs, T, lo_off);
+        note_launch();
+        const long long warps = (long long)A.reduces.size() * njt * 64;
+        tslice_tb_kernel<kNS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            A.d_reduces, (int)A.reduces.size(), T, lo_off, nrhs, njt, ts, tstride, texp);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    if (!A.tile_row0.empty()) {
+        double fl = 0, by = 0;
+        for (const XTerm &t : A.xterms) {
+            fl += 2.0 * tc2::M * t.K * nrhs;
+            by += 2.0 * kNS * ((double)tc2::M * pad16(t.K)) + 2.0 * kNS * pad16(t.K) * nrhs;
+        }
+        ProfScope ps("sliced_expand", st, fl * npairs, by + 16.0 * m * nrhs);
+        launch_expand_tb<kNS, kD>(p, A, S->pool, S->stride, S->exps, ts, tstride, texp, S->xs, m, S->xexp, nrhs,
+                                  true, B, ldb, true, R, ldr, st);
+        DG_CUDA(cudaGetLastError());
+    }
+    return 0;
+}
+
+// -------------------------------------------------- mixed inner solve
+template <int NS>
+static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
+{
+    const int m = p->m;
+    const int nlev = (int)F->lv.size();
+    std::vector<int> ev_off(p->lr.size()), ez_off(nlev), el_off(p->leaves.size());
+    int nexp = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        ev_off[b] = nexp;
+        nexp += p->lr[b].rank;
+    }
+    for (int l = 0; l < nlev; ++l) {
+        ez_off[l] = nexp;
+        nexp += m;
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        el_off[i] = nexp;
+        nexp += p->leaves[i].b;
+    }
+    VLayout VL;
+    std::vector<std::array<long long, 4>> vdst;
+    std::vector<std::array<int, 4>> vnr;
+    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL);
+    std::vector<long long> za(nlev, 0), la(p->leaves.size(), 0);
+    std::vector<int> nkbw(nlev, 0);
+    std::vector<RSliceJob> zj, lj;
+    std::vector<int> zb, lb;
+    int zr = 0, lr = 0;
+    for (int l = 0; l < nlev; ++l) {
+        const int w = F->lv[l].width;
+        nkbw[l] = (w + 15) / 16;
+        za[l] = el;
+        el += (long long)(m / tc2::M) * nkbw[l] * kTbA;
+        if (w == 0) continue;
+        zb.push_back(zr);
+        zj.push_back(RSliceJob{F->zoff[l], za[l], m, m, w, nkbw[l], ez_off[l]});
+        zr += m;
+    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        la[i] = el;
+        el += (long long)(L.b / tc2::M) * (L.b / 16) * kTbA;
+        lb.push_back(lr);
+        lj.push_back(RSliceJob{F->leafoff[i], la[i], L.b, L.b, L.b, L.b / 16, el_off[i]});
+        lr += L.b;
+    }
+    M->stride = al32(std::max<long long>(el, 1));
+    if (cudaMalloc((void **)&M->pool, (size_t)NS * M->stride * sizeof(bf16)) != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
+    M->bytes += (long long)NS * M->stride * 2;
+    DG_CUDA(cudaMemsetAsync(M->pool, 0, (size_t)NS * M->stride * sizeof(bf16), st));
+    int rc;
+    if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &M->exps, &M->bytes))) return rc;
+    {
+        VSliceJob *d_vj = nullptr;
+        RSliceJob *d_zj = nullptr, *d_lj = nullptr;
+        int *d_vb = nullptr, *d_zb = nullptr, *d_lb = nullptr;
+        long long tmp = 0;
+        if ((rc = dev_vec(VL.jobs, &d_vj, &tmp)) || (rc = dev_vec(VL.col_base, &d_vb, &tmp)) ||
+            (rc = dev_vec(zj, &d_zj, &tmp)) || (rc = dev_vec(zb, &d_zb, &tmp)) || (rc = dev_vec(lj, &d_lj, &tmp)) ||
+            (rc = dev_vec(lb, &d_lb, &tmp)))
+            return rc;
+        if (VL.ncols > 0) {
+            slice_v_tb_kernel<NS><<<VL.ncols, 256, 0, st>>>(d_vj, d_vb, (int)VL.jobs.size(), p->pool, M->pool,
+                                                           M->stride, M->exps);
+            note_launch();
+        }
+        if (zr > 0) {
+            slice_r_tb_kernel<NS><<<(zr + 127) / 128, 128, 0, st>>>(d_zj, d_zb, (int)zj.size(), zr, F->zpool,
+                                                                   M->pool, M->stride, M->exps);
+            note_launch();
+        }
+        if (lr > 0) {
+            slice_r_tb_kernel<NS><<<(lr + 127) / 128, 128, 0, st>>>(d_lj, d_lb, (int)lj.size(), lr, F->leafinv,
+                                                                   M->pool, M->stride, M->exps);
+            note_launch();
+        }
+        cudaError_t e2 = cudaGetLastError();
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+        cudaFree(d_vj);
+        cudaFree(d_vb);
+        cudaFree(d_zj);
+        cudaFree(d_zb);
+        cudaFree(d_lj);
+        cudaFree(d_lb);
+        if (e2 != cudaSuccess) return fail(DPLR_GPU_ECUDA, "mixed slicing: %s", cudaGetErrorString(e2));
+    }
+    // W tile-block offsets over all blocks (per 64-column rhs tile)
+    std::vector<long long> tpre(p->lr.size(), 0);
+    long long tp = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        tpre[b] = tp;
+        tp += (long long)((p->lr[b].rank + 15) / 16) * kTbB;
+    }
+    M->t_per_rhs = p->total_rank;
+    M->tpad_per_rhs = tp;             // per 64-column tile
+    M->nblocks = (int)p->lr.size();
+    M->level.resize(nlev);
+    for (int l = 0; l < nlev; ++l) {
+        SSchedule &S = M->level[l];
+        S.tile_m = tc2::M;
+        S.tpre = tp;
+        long long poff = 0;
+        for (int b : F->lv[l].blocks) {
+            const LRDesc &L = p->lr[b];
+            if (L.rank == 0) continue;
+            panel_items(L, vdst[b], vnr[b], poff, S.pitems);
+            const int nch = (L.n + 1023) / 1024;
+            const int ridx = (int)S.reduces.size();
+            S.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], pad16(L.rank), tpre[b]});
+            poff += (long long)nch * L.rank;
+            S.max_rank = std::max(S.max_rank, L.rank);
+            for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += tc2::M) {
+                S.tile_row0.push_back(t0);
+                S.tile_begin.push_back((int)S.xterms.size());
+                S.xterms.push_back(XTerm{za[l] + (long long)(t0 / tc2::M) * nkbw[l] * kTbA, tpre[b], L.rank,
+                                         ez_off[l] + t0, 0, ridx});
+            }
+        }
+        S.tile_begin.push_back((int)S.xterms.size());
+        S.partial_per_rhs = poff;
+        S.t_per_rhs = p->total_rank;
+        if ((rc = upload_tb(S, &M->bytes))) return rc;
+    }
+    SSchedule &LS = M->leaf;
+    LS.tile_m = tc2::M;
+    for (size_t i = 0; i < p->leaves.size(); ++i) {
+        const LeafDesc &L = p->leaves[i];
+        for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += tc2::M) {
+            LS.tile_row0.push_back(t0);
+            LS.tile_begin.push_back((int)LS.xterms.size());
+            LS.xterms.push_back(XTerm{la[i] + (long long)((t0 - L.row0) / tc2::M) * (L.b / 16) * kTbA, L.row0 / 16,
+                                      L.b, el_off[i] + (t0 - L.row0), 1, -1});
+        }
+    }
+    LS.tile_begin.push_back((int)LS.xterms.size());
+    if ((rc = upload_tb(LS, &M->bytes))) return rc;
+    if ((rc = ensure_err_flag(p))) return rc;
+    return tb_attrs<NS, NS + 1>();
+}
+
+template <int NS>
+static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const double *B, int ldb, double *X, int ldx,
+                          cudaStream_t st)
+{
+    constexpr int D = NS + 1;
+    const int m = p->m;
+    const int njt = (nrhs + 63) / 64;
+    // scratch: partials, DD T, W, W slices, W exponents
+    auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    long long part = 0;
+    for (const SSchedule &L : M->level) part = std::max(part, L.partial_per_rhs);
+    size_t maxred = 1;
+    for (const SSchedule &L : M->level) maxred = std::max(maxred, L.reduces.size());
+    const size_t part_bytes = r256((size_t)part * nrhs * sizeof(__int128));
+    const size_t t_bytes = r256((size_t)2 * M->t_per_rhs * nrhs * sizeof(double));
+    const size_t w_bytes = r256((size_t)M->t_per_rhs * nrhs * sizeof(double));
+    const long long wstride = M->tpad_per_rhs * njt;
+    const size_t ws_bytes = r256((size_t)NS * wstride * sizeof(bf16));
+    const size_t we_bytes = r256(maxred * nrhs * sizeof(int));
+    const size_t need = part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes;
+    if (M->work_bytes < need) {
+        cudaFree(M->work);
+        M->work = nullptr;
+        M->work_bytes = 0;
+        if (cudaMalloc(&M->work, need) != cudaSuccess) return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate scratch");
+        M->work_bytes = need;
+    }
+    char *base = reinterpret_cast<char *>(M->work);
+    __int128 *partials = reinterpret_cast<__int128 *>(base);
+    double *T = reinterpret_cast<double *>(base + part_bytes);
+    const long long lo_off = M->t_per_rhs * nrhs;
+    double *W = reinterpret_cast<double *>(base + part_bytes + t_bytes);
+    bf16 *ws = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes + w_bytes);
+    int *wexp = reinterpret_cast<int *>(base + part_bytes + t_bytes + w_bytes + ws_bytes);
+    const double npairs = pair_count(NS, D);
+    int rc;
+
+    // leaf step: X = Leaf^-1 B
+    if ((rc = slice_x_tb<NS>(B, m, ldb, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+    {
+        const SSchedule &LS = M->leaf;
+        double fl = 0;
+        for (const XTerm &t : LS.xterms) fl += 2.0 * tc2::M * t.K * nrhs;
+        ProfScope ps("mixed_expand", st, fl * npairs, 0.0);
+        launch_expand_tb<NS, D>(p, LS, M->pool, M->stride, M->exps, ws, wstride, wexp, M->xs, m, M->xexp, nrhs, false,
+                                nullptr, 0, false, X, ldx, st);
+        DG_CUDA(cudaGetLastError());
+    }
+    for (int l = (int)M->level.size() - 1; l >= 0; --l) {
+        const SSchedule &S = M->level[l];
+        if (S.pitems.empty()) continue;
+        if ((rc = slice_x_tb<NS>(X, m, ldx, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+        double fl = 0;
+        for (const PItem &it : S.pitems) fl += 2.0 * it.nkb * 16 * std::min(64, it.rank - it.kt) * nrhs;
+        {
+            ProfScope ps("mixed_panel", st, fl * npairs, 0.0);
+            launch_panel_tb<NS, D>(p, S, M->pool, M->stride, M->xs, m, nrhs, partials, st);
+        }
+        const long long maxcnt = (long long)S.max_rank * nrhs;
+        sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+            S.d_reduces, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+        if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
+        const long long warps = (long long)S.reduces.size() * njt * 64;
+        tslice_tb_kernel<NS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            S.d_reduces, (int)S.reduces.size(), W, -1, nrhs, njt, ws, wstride, wexp);
+        note_launch();
+        double fu = 0;
+        for (const XTerm &t : S.xterms) fu += 2.0 * tc2::M * t.K * nrhs;
+        ProfScope ps2("mixed_expand", st, fu * npairs, 0.0);
+        launch_expand_tb<NS, D>(p, S, M->pool, M->stride, M->exps, ws, wstride, wexp, M->xs, m, M->xexp, nrhs, true, X,
+                                ldx, true, X, ldx, st);
+        DG_CUDA(cudaGetLastError());
+    }
+    return 0;
+}
+
 
 }  // namespace dg

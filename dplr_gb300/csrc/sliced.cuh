@@ -54,8 +54,37 @@ struct STerm {
     int ldb, x_row0, blk;
 };
 
+// Tile-block schedules of the tcgen05 pipeline kernels (tcpipe.cuh).  A
+// tile-block is R rows x 16 inner elements of one slice, contiguous, in the
+// tensor core's K-major core-matrix order.
+struct XTerm {          // term of a 128-row expand tile
+    long long a;        // A tile-block of inner block 0 (slice 0); block kb at a + kb * 2048
+    long long b;        // src 0: T tile-block base of the block per 64-column rhs tile (times njt);
+                        // src 1: first X row-block
+    int K;              // inner length (16-element blocks: ceil(K / 16))
+    int aexp;           // exponent offset of the tile's row 0
+    int src;            // 0: T slices (exponents texp[blk * nrhs + j]), 1: X slices (xexp[j])
+    int blk;
+};
+
+struct PItem {          // panel work item: one row chunk of a block, one rank tile (<= 64)
+    long long v;        // V tile-blocks of (block, rank tile), slice 0: row-block rb at v + rb * nr * 16
+    long long p;        // partial offset / nrhs of the block
+    int rank, kt, nr;   // block rank, first rank of the tile, padded rows of its tile-blocks
+    int xrb0;           // first X row-block ((in0 + r0) / 16)
+    int vrb0;           // first V row-block of the chunk (r0 / 16)
+    int nkb;            // chunk rows / 16
+    int chunk;
+};
+
 struct SSchedule {
     int tile_m = 64;                // rows of an expand tile: 64 (mma.sync) or 128 (tcgen05)
+    // tcgen05 pipeline (tile_m == 128)
+    std::vector<PItem> pitems;
+    std::vector<XTerm> xterms;
+    long long tpre = 0;             // T tile-block elements of all blocks per 64-column rhs tile
+    PItem *d_pitems = nullptr;
+    XTerm *d_xterms = nullptr;
     std::vector<SPanelItem> items;
     std::vector<SReduceItem> reduces;
     long long partial_per_rhs = 0;

@@ -1,0 +1,628 @@
+// tcpipe.cuh -- warp-specialised persistent tcgen05 kernels for the
+// exact-slice products (second generation; the arithmetic is the one of
+// tcslice.cuh: one FP32 TMEM accumulator per slice diagonal, exact
+// read-out every 256 inner elements, 128-bit integer combination).
+//
+// Operand layout ("tile-blocks"): every slice of every operand is stored as
+// tile-blocks of R rows x 16 inner elements (R = 128 or 64, or the padded
+// rank of a panel tile), each contiguous and already in the canonical
+// K-major no-swizzle order of the tensor core (8-row x 16-byte core
+// matrices: element (r, k) at (r/8)*128 + (k/8)*64 + (r%8)*8 + k%8).  One
+// pipeline stage is therefore 2*NS contiguous blocks, fetched with one
+// cp.async.bulk each into a ring of shared-memory stages.
+//
+// Roles (320 threads, one CTA per SM, persistent over work items):
+//   warp 0, lane 0: producer -- waits for a free stage, posts the stage's
+//       byte count on its `full` mbarrier and issues the bulk copies;
+//   warp 1, lane 0: MMA issuer -- waits for `full`, issues every slice pair
+//       of the stage (tcgen05.mma), commits to the stage's `empty` barrier;
+//       at the end of a 256-deep range it commits to `accf`;
+//   warps 2..9: epilogue -- wait for `accf`, read the diagonals out of TMEM,
+//       combine them exactly, release TMEM through `acce` (the next range's
+//       MMAs start while the epilogue finishes its integer work), and write
+//       the item's outputs.
+// Waits are bounded; an expired wait sets a CTA-wide abort flag that every
+// role polls, the kernel records an error, drains and frees TMEM.
+#pragma once
+
+#include "tcslice.cuh"
+
+namespace dg {
+namespace tc2 {
+
+using tc::ashift;
+using tc::commit;
+using tc::fence_after;
+using tc::fence_before;
+using tc::fint;
+using tc::ld8;
+using tc::ld_wait;
+using tc::su32;
+
+constexpr int KB = 16;                 // inner elements per stage
+constexpr int M = 128, N = 64;
+constexpr int RANGE = 16;              // stages per exact read-out (256 inner elements)
+constexpr int TB_A = M * KB;           // elements of a 128-row tile-block
+constexpr int TB_B = N * KB;           // elements of a 64-row tile-block
+constexpr int THREADS = 320;
+constexpr int kSmem = 192 * 1024;
+constexpr int kSpin = 1 << 22;
+
+template <int NS>
+struct Cfg {
+    static constexpr int STAGE = NS * (TB_A + TB_B) * 2;                    // bytes
+    static constexpr int NST = (kSmem / STAGE) > 8 ? 8 : (kSmem / STAGE);
+    static constexpr int SMEM = NST * STAGE;
+};
+
+// Element offset of (r, k) inside a tile-block.
+__host__ __device__ constexpr int tbo(int r, int k)
+{
+    return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+constexpr uint32_t kIdescM128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(M >> 4) << 24);
+__device__ __forceinline__ uint32_t idesc_n(int n) { return kIdescM128 | ((uint32_t)(n >> 3) << 17); }
+
+// LBO 128 B (next 8 inner elements), SBO 256 B (next 8 rows).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void mma_n(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(su32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+
+// 32 lanes x 4 consecutive columns.
+__device__ __forceinline__ void ld4(uint32_t taddr, uint32_t (&r)[4])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+
+// Exact read-out of 4 columns (c4-th group of this warp's 32) of every
+// diagonal: W = ghi * 2^28 + glo in units 2^-7D (see tcslice.cuh).
+template <int D>
+__device__ __forceinline__ void read4(uint32_t trow, int c4, __int128 (&W)[4])
+{
+    constexpr int DH = D >= 6 ? D - 4 : 1;
+    long long ghi[4], glo[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ghi[u] = glo[u] = 0;
+    if (DH >= 2) {
+        uint32_t r[DH >= 2 ? DH - 1 : 1][4];
+#pragma unroll
+        for (int d = 2; d <= DH; ++d) ld4(trow + (uint32_t)((d - 2) * N + c4 * 4), r[d - 2]);
+        ld_wait();
+#pragma unroll
+        for (int d = 2; d <= DH; ++d)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) ghi[u] += fint(r[d - 2][u], 7 * (D - 4 - d));
+    }
+    {
+        constexpr int D0 = DH + 1;
+        uint32_t r[D - D0 + 1][4];
+#pragma unroll
+        for (int d = D0; d <= D; ++d) ld4(trow + (uint32_t)((d - 2) * N + c4 * 4), r[d - D0]);
+        ld_wait();
+#pragma unroll
+        for (int d = D0; d <= D; ++d)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) glo[u] += fint(r[d - D0][u], 7 * (D - d));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) W[u] = (DH >= 2 ? ((__int128)ghi[u] << 28) : (__int128)0) + glo[u];
+}
+
+// Same read-out for D <= 7 as one 64-bit integer per column (the exact sum
+// stays below 2^62: six diagonals of |I| < 2^24 shifted by at most 35).
+template <int D>
+__device__ __forceinline__ void read4_64(uint32_t trow, int c4, long long (&W)[4])
+{
+    static_assert(D <= 7, "64-bit read-out holds at most six diagonals");
+    uint32_t r[D - 1][4];
+#pragma unroll
+    for (int d = 2; d <= D; ++d) ld4(trow + (uint32_t)((d - 2) * N + c4 * 4), r[d - 2]);
+    ld_wait();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        long long w = 0;
+#pragma unroll
+        for (int d = 2; d <= D; ++d) w += fint(r[d - 2][u], 7 * (D - d));
+        W[u] = w;
+    }
+}
+
+// v * 2^E rounded to nearest with integer arithmetic (|v| < 2^63).
+__device__ __forceinline__ double i64_scaled(long long v, int E)
+{
+    if (v == 0) return 0.0;
+    const bool neg = v < 0;
+    unsigned long long a = neg ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int msb = 63 - __clzll((long long)a);
+    unsigned long long mant;
+    int e;
+    if (msb <= 52) {
+        mant = a << (52 - msb);
+        e = E - (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        mant = a >> sh;
+        const unsigned long long rem = a & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+        e = E + sh;
+        if (rem > half || (rem == half && (mant & 1ULL))) {
+            ++mant;
+            if (mant == (1ULL << 53)) {
+                mant >>= 1;
+                ++e;
+            }
+        }
+    }
+    const int be = e + 52 + 1023;
+    if (be >= 1 && be <= 2046)
+        return __longlong_as_double((long long)(((unsigned long long)be << 52) | (mant & ((1ULL << 52) - 1)) |
+                                                (neg ? (1ULL << 63) : 0ULL)));
+    const double r = ldexp((double)mant, e);
+    return neg ? -r : r;
+}
+
+struct Ctl {
+    uint64_t full[8], empty[8];
+    uint64_t accf, acce;
+    uint32_t tmem;
+    volatile int abort;
+};
+
+// Bounded wait; false (and the CTA-wide abort flag set) on expiry or when
+// another role aborted.
+__device__ __forceinline__ bool wait_bar(Ctl &c, uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = su32(bar);
+    for (int it = 0; it < kSpin; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (c.abort) return false;
+    }
+    c.abort = 1;
+    return false;
+}
+
+// Bounded wait that ignores the abort flag (draining after an abort).
+__device__ __forceinline__ void wait_raw(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = su32(bar);
+    for (int it = 0; it < kSpin; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return;
+    }
+}
+
+// All slice pairs p + q <= D of one stage (A: NS blocks of 128 rows, B: NS
+// blocks of `nb` rows), diagonal d into TMEM columns (d - 2) * 64.
+template <int NS, int D>
+__device__ __forceinline__ void issue(uint32_t tmem, uint32_t a0, uint32_t b0, int nb, uint32_t idesc, bool first)
+{
+#pragma unroll 1
+    for (int d = 2; d <= D; ++d) {
+        const int plo = d - NS > 1 ? d - NS : 1, phi = d - 1 < NS ? d - 1 : NS;
+#pragma unroll
+        for (int p = plo; p <= phi; ++p) {
+            const uint64_t ad = sdesc(a0 + (uint32_t)((p - 1) * TB_A * 2));
+            const uint64_t bd = sdesc(b0 + (uint32_t)((d - p - 1) * nb * KB * 2));
+            mma_n(tmem + (uint32_t)((d - 2) * N), ad, bd, idesc, (first && p == plo) ? 0u : 1u);
+        }
+    }
+}
+
+template <int NS, int D>
+__device__ __forceinline__ void setup(Ctl &ctl, int warp, int lane)
+{
+    if (warp == 0 && lane == 0) {
+        for (int s = 0; s < Cfg<NS>::NST; ++s) {
+            tc::mbar_init(&ctl.full[s], 1);
+            tc::mbar_init(&ctl.empty[s], 1);
+        }
+        tc::mbar_init(&ctl.accf, 1);
+        tc::mbar_init(&ctl.acce, 8);
+        ctl.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&ctl.tmem)),
+                     "r"(tc::tmem_cols(D)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+}
+
+// Teardown.  After an abort the producer waits (bounded) for the copies
+// still in flight (the last fill of each stage) and the MMA lane for its
+// last committed MMAs; then TMEM is freed.
+template <int NS, int D>
+__device__ __forceinline__ void teardown(Ctl &ctl, int warp, int lane, int issued, int consumed, int *err)
+{
+    if (ctl.abort && lane == 0) {
+        if (warp == 0)
+            for (int k = issued > Cfg<NS>::NST ? issued - Cfg<NS>::NST : 0; k < issued; ++k)
+                wait_raw(&ctl.full[k % Cfg<NS>::NST], (uint32_t)((k / Cfg<NS>::NST) & 1));
+        if (warp == 1 && consumed > 0)
+            wait_raw(&ctl.empty[(consumed - 1) % Cfg<NS>::NST], (uint32_t)(((consumed - 1) / Cfg<NS>::NST) & 1));
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (ctl.abort && threadIdx.x == 0) tc::record_error(err, 2);
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(ctl.tmem),
+                                "r"(tc::tmem_cols(D)));
+}
+
+// ------------------------------------------------------------- expand
+__device__ __forceinline__ int nkb_of(int K) { return (K + KB - 1) / KB; }
+
+// Y[tile, 64 columns] = (-1)^neg sum_terms A_t B_t (+ Bin).  Work item
+// it = tile * njt + jt (right-hand-side tiles of one row tile adjacent).
+// LEAN (D <= 7, every tile a single term, as in the inner solve): the exact
+// product of each output is one 64-bit integer, rounded once to FP64 and
+// added to Bin in FP64 (accurate to the inner solve's 43 bits); otherwise
+// all terms and Bin meet in a 128-bit fixed-point sum rounded once.
+template <int NS, int D, bool LEAN>
+__global__ void __launch_bounds__(THREADS, 1)
+    expand_kernel(const XTerm *__restrict__ terms, const int *__restrict__ tile_row0,
+                  const int *__restrict__ tile_begin, int ntiles, int njt, const bf16 *__restrict__ apool,
+                  long long astride, const int *__restrict__ aexp, const bf16 *__restrict__ ts, long long tstride,
+                  const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int xnjt,
+                  const int *__restrict__ xexp, int nrhs, int neg, const double *__restrict__ Bin, int ldbin,
+                  int addb, double *__restrict__ Y, int ldy, int *err)
+{
+    using C = Cfg<NS>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ Ctl ctl;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    setup<NS, D>(ctl, warp, lane);
+    const uint32_t sbase = su32(smem);
+    const int nitems = ntiles * njt;
+    int issued = 0, consumed = 0;
+
+    if (warp == 0) {
+        // ---------------------------------------------------- producer
+        if (lane == 0) {
+            for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
+                const int tile = it / njt, jt = it % njt;
+                for (int q = tile_begin[tile]; q < tile_begin[tile + 1] && !ctl.abort; ++q) {
+                    const XTerm tt = terms[q];
+                    const int nkb = nkb_of(tt.K);
+                    for (int kb = 0; kb < nkb; ++kb) {
+                        const int s = issued % C::NST, f = issued / C::NST;
+                        if (f > 0 && !wait_bar(ctl, &ctl.empty[s], (uint32_t)((f - 1) & 1))) break;
+                        expect_tx(&ctl.full[s], (uint32_t)C::STAGE);
+                        const uint32_t da = sbase + (uint32_t)(s * C::STAGE), db = da + NS * TB_A * 2;
+#pragma unroll 1
+                        for (int p = 0; p < NS; ++p)
+                            bulk_g2s(da + p * TB_A * 2, apool + p * astride + tt.a + (long long)kb * TB_A, TB_A * 2,
+                                     &ctl.full[s]);
+                        const long long boff = tt.src == 0 ? tt.b * njt + ((long long)jt * nkb + kb) * TB_B
+                                                           : ((tt.b + kb) * (long long)xnjt + jt) * TB_B;
+                        const bf16 *bsrc = tt.src == 0 ? ts : xs;
+                        const long long bstr = tt.src == 0 ? tstride : xstride;
+#pragma unroll 1
+                        for (int p = 0; p < NS; ++p)
+                            bulk_g2s(db + p * TB_B * 2, bsrc + p * bstr + boff, TB_B * 2, &ctl.full[s]);
+                        ++issued;
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t tmem = ctl.tmem;
+            const uint32_t idesc = idesc_n(N);
+            int rc = 0;
+            for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
+                const int tile = it / njt;
+                for (int q = tile_begin[tile]; q < tile_begin[tile + 1] && !ctl.abort; ++q) {
+                    const int nkb = nkb_of(terms[q].K);
+                    for (int kb0 = 0; kb0 < nkb && !ctl.abort; kb0 += RANGE) {
+                        if (rc > 0 && !wait_bar(ctl, &ctl.acce, (uint32_t)((rc - 1) & 1))) break;
+                        const int kb1 = min(nkb, kb0 + RANGE);
+                        for (int kb = kb0; kb < kb1; ++kb) {
+                            const int s = consumed % C::NST;
+                            if (!wait_bar(ctl, &ctl.full[s], (uint32_t)((consumed / C::NST) & 1))) break;
+                            fence_after();
+                            const uint32_t a0 = sbase + (uint32_t)(s * C::STAGE);
+                            issue<NS, D>(tmem, a0, a0 + NS * TB_A * 2, N, idesc, kb == kb0);
+                            commit(&ctl.empty[s]);
+                            ++consumed;
+                        }
+                        if (ctl.abort) break;
+                        commit(&ctl.accf);
+                        ++rc;
+                    }
+                }
+            }
+        }
+    } else {
+        // ---------------------------------------------------- epilogue
+        const int lq = warp & 3, ch = (warp - 2) >> 2;
+        const int row = lq * 32 + lane;
+        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * 32);
+        int ec = 0;
+        if constexpr (LEAN) {
+            for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
+                const int tile = it / njt, jt = it % njt;
+                const int q0 = tile_begin[tile];
+                const int j0 = jt * N + ch * 32, myj = j0 + lane;
+                const XTerm tt = terms[q0];
+                const int nkb = nkb_of(tt.K);
+                const int re = aexp[tt.aexp + row] - 7 * D;
+                const int cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
+                long long acc[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) acc[c] = 0;
+                bool ok = true;
+                for (int kb0 = 0; kb0 < nkb; kb0 += RANGE) {
+                    if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+#pragma unroll
+                    for (int c4 = 0; c4 < 8; ++c4) {
+                        long long W[4];
+                        read4_64<D>(trow, c4, W);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) acc[c4 * 4 + u] += W[u];
+                    }
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) arrive(&ctl.acce);
+                    ++ec;
+                }
+                if (!ok) break;
+                const int gr = tile_row0[tile] + row;
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const int j = j0 + c;
+                    const int ce = __shfl_sync(0xffffffffu, cel, c);
+                    if (j < nrhs) {
+                        const double t = i64_scaled(neg ? -acc[c] : acc[c], re + ce);
+                        Y[gr + (long long)j * ldy] = addb ? Bin[gr + (long long)j * ldbin] + t : t;
+                    }
+                }
+            }
+        } else
+        for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
+            const int tile = it / njt, jt = it % njt;
+            const int q0 = tile_begin[tile], q1 = tile_begin[tile + 1];
+            const int j0 = jt * N + ch * 32;         // this warp's first column
+            const int myj = j0 + lane;               // column whose exponents this lane holds
+            int rmax = -100000, cmaxl = -100000;
+            for (int q = q0; q < q1; ++q) {
+                const XTerm &tt = terms[q];
+                rmax = max(rmax, aexp[tt.aexp + row]);
+                if (myj < nrhs) cmaxl = max(cmaxl, tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]);
+            }
+            if (rmax < -99999) rmax = 0;
+            if (cmaxl < -99999) cmaxl = 0;
+            __int128 acc[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) acc[c] = 0;
+            bool ok = true;
+            for (int q = q0; q < q1 && ok; ++q) {
+                const XTerm tt = terms[q];
+                const int nkb = nkb_of(tt.K);
+                const int rdel = aexp[tt.aexp + row] - rmax + 109 - 7 * D;
+                const int cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
+                const int cdl = cel - cmaxl;         // this lane's column shift part
+                for (int kb0 = 0; kb0 < nkb; kb0 += RANGE) {
+                    if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+#pragma unroll
+                    for (int c4 = 0; c4 < 8; ++c4) {
+                        __int128 W[4];
+                        read4<D>(trow, c4, W);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int sh = rdel + __shfl_sync(0xffffffffu, cdl, c4 * 4 + u);
+                            acc[c4 * 4 + u] += ashift(W[u], sh);
+                        }
+                    }
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) arrive(&ctl.acce);
+                    ++ec;
+                }
+            }
+            if (!ok) break;
+            // outputs: fold in +-Bin exactly, round once
+            const int gr = tile_row0[tile] + row;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const int j = j0 + c;
+                const int cm = __shfl_sync(0xffffffffu, cmaxl, c);
+                if (j < nrhs) {
+                    const int U = rmax + cm - 109;
+                    __int128 v = neg ? -acc[c] : acc[c];
+                    double out;
+                    if (addb) {
+                        const double b = Bin[gr + (long long)j * ldbin];
+                        const long long bits = __double_as_longlong(b);
+                        int eb = (int)((bits >> 52) & 0x7FF);
+                        long long mb = bits & ((1LL << 52) - 1);
+                        if (eb == 0x7FF) {
+                            out = b + tc::i128_to_double(v, U);
+                        } else {
+                            if (eb) mb |= 1LL << 52; else eb = 1;
+                            const int sb = eb - 1075 - U;
+                            if (sb <= 70) {
+                                const __int128 bm = ashift((__int128)mb, sb);
+                                v += bits < 0 ? -bm : bm;
+                                out = tc::i128_to_double(v, U);
+                            } else {
+                                out = b + tc::i128_to_double(v, U);
+                            }
+                        }
+                    } else {
+                        out = tc::i128_to_double(v, U);
+                    }
+                    Y[gr + (long long)j * ldy] = out;
+                }
+            }
+        }
+    }
+    teardown<NS, D>(ctl, warp, lane, issued, consumed, err);
+}
+
+// ------------------------------------------------------------- panel
+// Work unit it = item * njp + jp (pairs of 64-column X tiles adjacent).
+template <int NS, int D>
+__global__ void __launch_bounds__(THREADS, 1)
+    panel_kernel(const PItem *__restrict__ items, int nitems, int njp, const bf16 *__restrict__ vpool,
+                 long long vstride, const bf16 *__restrict__ xs, long long xstride, int xnjt, int nrhs,
+                 __int128 *__restrict__ partials, int *err)
+{
+    using C = Cfg<NS>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ Ctl ctl;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    setup<NS, D>(ctl, warp, lane);
+    const uint32_t sbase = su32(smem);
+    const int nunits = nitems * njp;
+    int issued = 0, consumed = 0;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int u = blockIdx.x; u < nunits && !ctl.abort; u += gridDim.x) {
+                const PItem itm = items[u / njp];
+                const int jp = u % njp;
+                const uint32_t bbytes = (uint32_t)(itm.nr * KB * 2);
+                for (int kb = 0; kb < itm.nkb; ++kb) {
+                    const int s = issued % C::NST, f = issued / C::NST;
+                    if (f > 0 && !wait_bar(ctl, &ctl.empty[s], (uint32_t)((f - 1) & 1))) break;
+                    expect_tx(&ctl.full[s], (uint32_t)NS * (TB_A * 2 + bbytes));
+                    const uint32_t da = sbase + (uint32_t)(s * C::STAGE), db = da + NS * TB_A * 2;
+                    const long long aoff = ((long long)(itm.xrb0 + kb) * xnjt + 2 * jp) * TB_B;   // two 64-row blocks
+#pragma unroll 1
+                    for (int p = 0; p < NS; ++p) bulk_g2s(da + p * TB_A * 2, xs + p * xstride + aoff, TB_A * 2, &ctl.full[s]);
+                    const long long boff = itm.v + (long long)(itm.vrb0 + kb) * itm.nr * KB;
+#pragma unroll 1
+                    for (int p = 0; p < NS; ++p)
+                        bulk_g2s(db + p * bbytes, vpool + p * vstride + boff, bbytes, &ctl.full[s]);
+                    ++issued;
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t tmem = ctl.tmem;
+            int rc = 0;
+            for (int u = blockIdx.x; u < nunits && !ctl.abort; u += gridDim.x) {
+                const PItem itm = items[u / njp];
+                const uint32_t idesc = idesc_n(itm.nr);
+                for (int kb0 = 0; kb0 < itm.nkb && !ctl.abort; kb0 += RANGE) {
+                    if (rc > 0 && !wait_bar(ctl, &ctl.acce, (uint32_t)((rc - 1) & 1))) break;
+                    const int kb1 = min(itm.nkb, kb0 + RANGE);
+                    for (int kb = kb0; kb < kb1; ++kb) {
+                        const int s = consumed % C::NST;
+                        if (!wait_bar(ctl, &ctl.full[s], (uint32_t)((consumed / C::NST) & 1))) break;
+                        fence_after();
+                        const uint32_t a0 = sbase + (uint32_t)(s * C::STAGE);
+                        issue<NS, D>(tmem, a0, a0 + NS * TB_A * 2, itm.nr, idesc, kb == kb0);
+                        commit(&ctl.empty[s]);
+                        ++consumed;
+                    }
+                    if (ctl.abort) break;
+                    commit(&ctl.accf);
+                    ++rc;
+                }
+            }
+        }
+    } else {
+        const int lq = warp & 3, ch = (warp - 2) >> 2;
+        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * 32);
+        int ec = 0;
+        for (int u = blockIdx.x; u < nunits && !ctl.abort; u += gridDim.x) {
+            const PItem itm = items[u / njp];
+            const int jp = u % njp;
+            const int ncol = min(itm.nr, itm.rank - itm.kt);     // live ranks of the tile
+            __int128 acc[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) acc[c] = 0;
+            bool ok = true;
+            for (int kb0 = 0; kb0 < itm.nkb; kb0 += RANGE) {
+                if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
+                    ok = false;
+                    break;
+                }
+                fence_after();
+                // columns past the tile's padded rank hold stale values; they
+                // are read (the loads are warp-collective) but never written
+#pragma unroll
+                for (int c4 = 0; c4 < 8; ++c4) {
+                    __int128 W[4];
+                    read4<D>(trow, c4, W);
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[c4 * 4 + v] += W[v];
+                }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) arrive(&ctl.acce);
+                ++ec;
+            }
+            if (!ok) break;
+            const int j = jp * M + lq * 32 + lane;                 // right-hand side of this lane
+            if (j < nrhs) {
+                __int128 *P = partials + itm.p * nrhs + (long long)itm.chunk * itm.rank * nrhs +
+                              (long long)j * itm.rank + itm.kt + ch * 32;
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (ch * 32 + c < ncol) P[c] = acc[c];
+            }
+        }
+    }
+    teardown<NS, D>(ctl, warp, lane, issued, consumed, err);
+}
+
+}  // namespace tc2
+}  // namespace dg
