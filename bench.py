@@ -424,11 +424,20 @@ def run_ours(args):
         bf16_peak, peak_src = float(peaks["bf16_tflops_sustained"]), "of measured (sustained bf16)"
     except Exception:
         bf16_peak, peak_src = 1700.0, "of fallback (sustained bf16)"
+    # DRAM traffic per launch of the dominant kernel, from the ncu capture summarised
+    # in profiles/ (scaled to a full-size launch by the units it processes)
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic_per_launch.json")))
+        if name in tr and tr[name].get("n") == args.n and tr[name].get("rhs") == args.rhs:
+            traffic = tr[name]["bytes"]
+    except Exception:
+        traffic = None
     if name.startswith(("sliced_", "mixed_")):
         roofline = {"kernel": name, "bound": "tensor", "achieved": tflops, "peak": bf16_peak,
-                    "unit": "TFLOP/s", "frac": tflops / bf16_peak, "traffic": None,
+                    "unit": "TFLOP/s", "frac": tflops / bf16_peak, "traffic": traffic,
                     "algorithmic_gbs": gbs, "share_of_timed": kms / ms, "peak_source": peak_src,
-                    "note": "bf16 MMA flops of all slice pairs (mma.sync m16n8k16)"}
+                    "note": "bf16 MMA flops of all slice pairs (tcgen05.mma kind::f16, 128-row tiles)"}
     else:
         roofline = {"kernel": name, "bound": "fp64", "achieved": tflops, "peak": fp64_peak,
                     "unit": "TFLOP/s", "frac": tflops / fp64_peak, "traffic": None,

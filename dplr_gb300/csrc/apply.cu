@@ -134,13 +134,23 @@ __global__ void __launch_bounds__(kThreads) panel1_kernel(const PanelItem *__res
                 }
             }
         }
+        // butterfly reduction of the four column sums: two exchange rounds
+        // leave lane l with the partial of column (l >> 3) & 3, three more
+        // finish it (6 FP64 adds per lane instead of 20)
+        {
+            const bool hi16 = lane & 16, hi8 = lane & 8;
+            const double s0 = hi16 ? acc[0] : acc[2], s1 = hi16 ? acc[1] : acc[3];
+            double a0 = (hi16 ? acc[2] : acc[0]) + __shfl_xor_sync(0xffffffffu, s0, 16);
+            double a1 = (hi16 ? acc[3] : acc[1]) + __shfl_xor_sync(0xffffffffu, s1, 16);
+            // lanes < 16 now hold columns {0, 1}, lanes >= 16 columns {2, 3}
+            const double t = hi8 ? a0 : a1;
+            double v = (hi8 ? a1 : a0) + __shfl_xor_sync(0xffffffffu, t, 8);
+            // lane l holds column 2*(l >= 16) + (l & 8 ? 1 : 0)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            double v = acc[c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            const int c = (hi16 ? 2 : 0) + (hi8 ? 1 : 0);
             const int k = k0 + c * (kThreads / 32);
-            if (lane == 0 && k < it.rank) P[k] = v;
+            if ((lane & 7) == 0 && k < it.rank) P[k] = v;
         }
     }
 }
@@ -195,6 +205,33 @@ __global__ void reduce_kernel(const ReduceItem *__restrict__ items,
     double s = 0.0;
     for (int c = 0; c < R.nch; ++c) s += P[(long long)c * cnt];
     T[R.t * nrhs + e] = (R.sig >= 0 && sigbase) ? sigbase[R.sig + k] * s : s;
+}
+
+// Few right-hand sides: the chunk sums of an element are spread over 8 warps
+// (32 elements x 8 chunk groups per CTA) instead of one thread walking all
+// chunks, whose dependent loads dominate when a block has hundreds of chunks.
+__global__ void reduce_grouped_kernel(const ReduceItem *__restrict__ items, const double *__restrict__ sigbase,
+                                      const double *__restrict__ partials, int nrhs, double *__restrict__ T)
+{
+    __shared__ double red[8][33];
+    const ReduceItem R = items[blockIdx.x];
+    const long long cnt = (long long)R.rank * nrhs;
+    const int el = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const long long e = (long long)blockIdx.y * 32 + el;
+    double s = 0.0;
+    if (e < cnt) {
+        const double *P = partials + R.p * nrhs + e;
+        for (int c = grp; c < R.nch; c += 8) s += P[(long long)c * cnt];
+    }
+    red[grp][el] = s;
+    __syncthreads();
+    if (grp == 0 && e < cnt) {
+        double t = 0.0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) t += red[g][el];
+        const int k = (int)(e % R.rank);
+        T[R.t * nrhs + e] = (R.sig >= 0 && sigbase) ? sigbase[R.sig + k] * t : t;
+    }
 }
 
 // ---------------------------------------------------------------- expand
@@ -448,6 +485,13 @@ int run_reduce(const Schedule &S, const double *sigbase, const double *partials,
         by += 8.0 * (r.nch + 1.0) * r.rank * nrhs;
     }
     ProfScope ps("reduce", st, fl, by);
+    if (nrhs < 8) {
+        const dim3 g2((unsigned)S.reduces.size(), (unsigned)((maxcnt + 31) / 32));
+        reduce_grouped_kernel<<<g2, 256, 0, st>>>(S.d_reduces, sigbase, partials, nrhs, T);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
     reduce_kernel<<<g, 256, 0, st>>>(S.d_reduces, sigbase, partials, nrhs, T);
     note_launch();
     DG_CUDA(cudaGetLastError());

@@ -285,20 +285,52 @@ __global__ void slice_rows_kernel(const RowSliceJob *jobs, const int *row_base, 
     }
 }
 
-// Right-hand sides: one exponent per column over all rows.
+// Right-hand sides: one exponent per column over all rows.  Each column is
+// split over gridDim.y CTAs whose exponents meet in an integer atomicMax
+// (exponent of the maximum = maximum of the exponents); CTAs whose part is
+// zero contribute nothing, and a column that stays at the initial value is
+// all zero and gets exponent 0.
+constexpr int kNoExp = -(1 << 24);
+
+__global__ void xcol_init_kernel(int *xexp, int nrhs)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nrhs) xexp[j] = kNoExp;
+}
+
 __global__ void xcol_exp_kernel(const double *X, int m, int ldx, int *xexp)
 {
-    __shared__ double red[512];
+    __shared__ double red[256];
     const double *col = X + (long long)blockIdx.x * ldx;
+    const int per = (m + gridDim.y - 1) / gridDim.y;
+    const int r0 = blockIdx.y * per, r1 = min(m, r0 + per);
     double v = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) v = fmax(v, fabs(col[i]));
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) v = fmax(v, fabs(col[i]));
     red[threadIdx.x] = v;
     __syncthreads();
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
         if (threadIdx.x < k) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + k]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) xexp[blockIdx.x] = scale_exp(red[0]);
+    if (threadIdx.x == 0 && red[0] > 0.0) atomicMax(xexp + blockIdx.x, scale_exp(red[0]));
+}
+
+__global__ void xcol_fix_kernel(int *xexp, int nrhs)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nrhs && xexp[j] == kNoExp) xexp[j] = 0;       // all-zero column
+}
+
+// Column exponents of an m x nrhs block: 16 CTAs per column.
+static void xcol_exps(const double *X, int m, int ldx, int nrhs, int *xexp, cudaStream_t st)
+{
+    xcol_init_kernel<<<(nrhs + 255) / 256, 256, 0, st>>>(xexp, nrhs);
+    note_launch();
+    const int parts = std::max(1, std::min(16, m / 4096));
+    xcol_exp_kernel<<<dim3((unsigned)nrhs, (unsigned)parts), 256, 0, st>>>(X, m, ldx, xexp);
+    note_launch();
+    xcol_fix_kernel<<<(nrhs + 255) / 256, 256, 0, st>>>(xexp, nrhs);
+    note_launch();
 }
 
 // One column per blockIdx.y, rows strided over the x-blocks.
@@ -948,8 +980,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
     const long long xstride = (long long)m * nrhs;
     {
         ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * kNS * m * nrhs);
-        xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, S->xexp);
-        note_launch();
+        xcol_exps(X, m, ldx, nrhs, S->xexp, st);
         xslice_kernel<kNS><<<xslice_grid(m, nrhs), 256, 0, st>>>(X, m, ldx, nrhs, S->xexp, S->xs, xstride);
         note_launch();
         DG_CUDA(cudaGetLastError());
@@ -1245,8 +1276,7 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
 template <int NS>
 static int slice_block(const double *X, int m, int ldx, int nrhs, bf16 *xs, int *xexp, cudaStream_t st)
 {
-    xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, xexp);
-    note_launch();
+    xcol_exps(X, m, ldx, nrhs, xexp, st);
     xslice_kernel<NS><<<xslice_grid(m, nrhs), 256, 0, st>>>(X, m, ldx, nrhs, xexp, xs, (long long)m * nrhs);
     note_launch();
     DG_CUDA(cudaGetLastError());
@@ -1671,8 +1701,7 @@ int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
         xexp_n = nrhs;
     }
-    xcol_exp_kernel<<<nrhs, 512, 0, st>>>(X, m, ldx, xexp);
-    note_launch();
+    xcol_exps(X, m, ldx, nrhs, xexp, st);
     const long long cnt = (long long)(m / 16) * xnjt * 64;
     const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 16);
     xslice_tb_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
@@ -2118,7 +2147,10 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
     int rc;
 
     // leaf step: X = Leaf^-1 B
-    if ((rc = slice_x_tb<NS>(B, m, ldb, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+    {
+        ProfScope ps("mixed_slice_x", st, 0.0, (8.0 + 2.0 * NS) * m * nrhs);
+        if ((rc = slice_x_tb<NS>(B, m, ldb, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+    }
     {
         const SSchedule &LS = M->leaf;
         double fl = 0;
@@ -2131,7 +2163,10 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
     for (int l = (int)M->level.size() - 1; l >= 0; --l) {
         const SSchedule &S = M->level[l];
         if (S.pitems.empty()) continue;
-        if ((rc = slice_x_tb<NS>(X, m, ldx, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+        {
+            ProfScope ps("mixed_slice_x", st, 0.0, (8.0 + 2.0 * NS) * m * nrhs);
+            if ((rc = slice_x_tb<NS>(X, m, ldx, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+        }
         double fl = 0;
         for (const PItem &it : S.pitems) fl += 2.0 * it.nkb * 16 * std::min(64, it.rank - it.kt) * nrhs;
         {
@@ -2139,15 +2174,21 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
             launch_panel_tb<NS, D>(p, S, M->pool, M->stride, M->xs, m, nrhs, partials, st);
         }
         const long long maxcnt = (long long)S.max_rank * nrhs;
-        sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
-            S.d_reduces, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off);
-        note_launch();
-        DG_CUDA(cudaGetLastError());
+        {
+            ProfScope ps("mixed_reduce", st, 0.0, 0.0);
+            sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+                S.d_reduces, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off);
+            note_launch();
+            DG_CUDA(cudaGetLastError());
+        }
         if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
-        const long long warps = (long long)S.reduces.size() * njt * 64;
-        tslice_tb_kernel<NS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
-            S.d_reduces, (int)S.reduces.size(), W, -1, nrhs, njt, ws, wstride, wexp);
-        note_launch();
+        {
+            ProfScope ps("mixed_reduce", st, 0.0, 0.0);
+            const long long warps = (long long)S.reduces.size() * njt * 64;
+            tslice_tb_kernel<NS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+                S.d_reduces, (int)S.reduces.size(), W, -1, nrhs, njt, ws, wstride, wexp);
+            note_launch();
+        }
         double fu = 0;
         for (const XTerm &t : S.xterms) fu += 2.0 * tc2::M * t.K * nrhs;
         ProfScope ps2("mixed_expand", st, fu * npairs, 0.0);

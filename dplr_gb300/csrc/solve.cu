@@ -171,7 +171,10 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
             if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
             if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
         }
-        if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
+        {
+            ProfScope ps("refine_norms", st, 0.0, 8.0 * m * n);
+            if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
+        }
         DG_CUDA(cudaMemcpyAsync(hr.data(), rn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         DG_CUDA(cudaStreamSynchronize(st));
         if ((rc = sliced_error(p))) return rc;
@@ -179,7 +182,10 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
         for (int j = 0; j < n; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
         if (worst <= tol || it >= maxiter) break;
         if ((rc = inner(R, m, D, m))) return rc;
-        if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
+        {
+            ProfScope ps("refine_update", st, 0.0, 24.0 * m * n);
+            if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
+        }
         ++it;
     }
     if (rel_resid) *rel_resid = worst;
