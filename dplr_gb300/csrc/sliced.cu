@@ -28,6 +28,7 @@ namespace dg {
 
 struct Fact;
 static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st);
+template <int NSR>
 static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int ldx, const double *B, int ldb,
                               double *R, int ldr, cudaStream_t st);
 template <int NS>
@@ -100,6 +101,16 @@ __device__ __forceinline__ long long scaled_int(double x, int sh)
     return bits < 0 ? -y : y;
 }
 
+// bf16 bits of a digit a (-128 <= a <= 128, the range of the slices),
+// exactly, with full-rate arithmetic: the float 2^23 + 128 + a is built from
+// its bit pattern, 2^23 + 128 subtracted, and the float's top 16 bits
+// (exact: <= 8 significant bits) kept.
+__device__ __forceinline__ uint32_t digit_bits(int a)
+{
+    const float f = __int_as_float(0x4B000080 + a) - 8388736.0f;
+    return __float_as_uint(f) >> 16;
+}
+
 // Balanced base-128 digits of y (|y| < 2^(7 NS)): y = sum_p a_p 2^(7 (NS - p)),
 // a_p in [-64, 63] for p > 1 and |a_1| <= 128; written as bf16 (exact).
 template <int NS>
@@ -114,7 +125,7 @@ __device__ __forceinline__ void int_slices(long long y, bf16 *out, long long str
     }
     a[0] = (int)y;
 #pragma unroll
-    for (int p = 0; p < NS; ++p) out[p * stride] = __float2bfloat16_rn((float)a[p]);
+    for (int p = 0; p < NS; ++p) out[p * stride] = __ushort_as_bfloat16((unsigned short)digit_bits(a[p]));
 }
 
 // Slices of x with |x| < 2^e: x = 2^e sum_p a_p 2^(-7p) up to 2^(e - 7 NS - 1).
@@ -971,7 +982,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
     Sliced *S = (Sliced *)p->sliced;
     if (!S) return fail(DPLR_GPU_ESTATE, "sliced residual: plan has no sliced factors");
     if (nrhs <= 0 || p->m == 0) return 0;
-    if (S->apply.tile_m == tc::M) return sliced_residual_tb(p, S, nrhs, X, ldx, B, ldb, R, ldr, st);
+    if (S->apply.tile_m == tc::M) return sliced_residual_tb<kNS>(p, S, nrhs, X, ldx, B, ldb, R, ldr, st);
     const int m = p->m;
     const SSchedule &A = S->apply;
     SWork w;
@@ -1481,24 +1492,32 @@ __global__ void slice_v_tb_kernel(const VSliceJob *jobs, const int *col_base, in
         slice_d<NS>(col[i], e, base + (long long)(i >> 4) * nr * 16 + tc2::tbo(r, i & 15), stride);
 }
 
-// Row-sliced operands into 128-row tile-blocks: one thread per row.
+// Row-sliced operands into 128-row tile-blocks.
 struct RSliceJob {
     long long src;          // column-major rows x cols (ld)
     long long dst;          // tile-block base
     int ld, rows, cols, nkb, exp;
 };
 
+__device__ __forceinline__ int find_job(const int *base, int njobs, int g)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (base[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Row slicing into 128-row tile-blocks: one thread per row, one exponent
+// per row.
 template <int NS>
 __global__ void slice_r_tb_kernel(const RSliceJob *jobs, const int *row_base, int njobs, int total, const double *src,
                                   bf16 *dst, long long stride, int *exps)
 {
     const int gr = blockIdx.x * blockDim.x + threadIdx.x;
     if (gr >= total) return;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) / 2;
-        if (row_base[mid] <= gr) lo = mid; else hi = mid - 1;
-    }
+    const int lo = find_job(row_base, njobs, gr);
     const RSliceJob &J = jobs[lo];
     const int r = gr - row_base[lo];
     double mx = 0.0;
@@ -1531,17 +1550,10 @@ __device__ __forceinline__ void store8(const long long (&y)[8], bf16 *out, long 
 #pragma unroll
     for (int p = 0; p < NS; ++p) {
         uint4 w;
-        uint32_t h[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint16_t lo16 = __bfloat16_as_ushort(__float2bfloat16_rn((float)a[2 * q][p]));
-            const uint16_t hi16 = __bfloat16_as_ushort(__float2bfloat16_rn((float)a[2 * q + 1][p]));
-            h[q] = (uint32_t)lo16 | ((uint32_t)hi16 << 16);
-        }
-        w.x = h[0];
-        w.y = h[1];
-        w.z = h[2];
-        w.w = h[3];
+        w.x = digit_bits(a[0][p]) | (digit_bits(a[1][p]) << 16);
+        w.y = digit_bits(a[2][p]) | (digit_bits(a[3][p]) << 16);
+        w.z = digit_bits(a[4][p]) | (digit_bits(a[5][p]) << 16);
+        w.w = digit_bits(a[6][p]) | (digit_bits(a[7][p]) << 16);
         *reinterpret_cast<uint4 *>(out + p * stride) = w;
     }
 }
@@ -1572,7 +1584,8 @@ __global__ void xslice_tb_kernel(const double *X, int m, int ldx, int nrhs, int 
 }
 
 // T / W (rank x nrhs per block, FP64 or double-double) into tile-blocks of
-// 64 columns x 16 ranks; one warp per (block, column j < njt * 64).
+// 64 columns x 16 ranks, one exponent per (block, column); one warp per
+// (block, column j < njt * 64).
 template <int NS>
 __global__ void tslice_tb_kernel(const SReduceItem *__restrict__ items, int nitems, const double *__restrict__ T,
                                  long long lo_off, int nrhs, int njt, bf16 *__restrict__ ts, long long tstride,
@@ -1792,27 +1805,28 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     std::vector<std::array<long long, 4>> vdst;
     std::vector<std::array<int, 4>> vnr;
     long long el = layout_v(p, vdst, vnr, 0, ev_off, VL);
+    // every U row and leaf row has its own exponent
     std::vector<long long> ua(p->lr.size(), 0), la(p->leaves.size(), 0);
-    std::vector<RSliceJob> rj;
-    std::vector<int> rbase;
-    int nrows = 0;
+    std::vector<RSliceJob> uj, lj;
+    std::vector<int> ubase, lbase;
+    int nurows = 0, nlrows = 0;
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
         const int nkb = (L.rank + 15) / 16;
         ua[b] = el;
         el += (long long)(L.n / tc2::M) * nkb * kTbA;
-        rbase.push_back(nrows);
-        rj.push_back(RSliceJob{L.u, ua[b], L.n, L.n, L.rank, nkb, eu_off[b]});
-        nrows += L.n;
+        ubase.push_back(nurows);
+        uj.push_back(RSliceJob{L.u, ua[b], L.n, L.n, L.rank, nkb, eu_off[b]});
+        nurows += L.n;
     }
     for (size_t i = 0; i < p->leaves.size(); ++i) {
         const LeafDesc &L = p->leaves[i];
         la[i] = el;
         el += (long long)(L.b / tc2::M) * (L.b / 16) * kTbA;
-        rbase.push_back(nrows);
-        rj.push_back(RSliceJob{L.d, la[i], L.b, L.b, L.b, L.b / 16, ed_off[i]});
-        nrows += L.b;
+        lbase.push_back(nlrows);
+        lj.push_back(RSliceJob{L.d, la[i], L.b, L.b, L.b, L.b / 16, ed_off[i]});
+        nlrows += L.b;
     }
     S->stride = al32(std::max<long long>(el, 1));
     if (cudaMalloc((void **)&S->pool, (size_t)kNS * S->stride * sizeof(bf16)) != cudaSuccess)
@@ -1824,28 +1838,36 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &S->exps, &S->bytes))) return rc;
     {
         VSliceJob *d_vj = nullptr;
-        RSliceJob *d_rj = nullptr;
-        int *d_vb = nullptr, *d_rb = nullptr;
+        RSliceJob *d_uj = nullptr, *d_lj = nullptr;
+        int *d_vb = nullptr, *d_ub = nullptr, *d_lb = nullptr;
         long long tmp = 0;
         if ((rc = dev_vec(VL.jobs, &d_vj, &tmp)) || (rc = dev_vec(VL.col_base, &d_vb, &tmp)) ||
-            (rc = dev_vec(rj, &d_rj, &tmp)) || (rc = dev_vec(rbase, &d_rb, &tmp)))
+            (rc = dev_vec(uj, &d_uj, &tmp)) || (rc = dev_vec(ubase, &d_ub, &tmp)) || (rc = dev_vec(lj, &d_lj, &tmp)) ||
+            (rc = dev_vec(lbase, &d_lb, &tmp)))
             return rc;
         if (VL.ncols > 0) {
             slice_v_tb_kernel<kNS><<<VL.ncols, 256, 0, st>>>(d_vj, d_vb, (int)VL.jobs.size(), p->pool, S->pool,
                                                             S->stride, S->exps);
             note_launch();
         }
-        if (nrows > 0) {
-            slice_r_tb_kernel<kNS><<<(nrows + 127) / 128, 128, 0, st>>>(d_rj, d_rb, (int)rj.size(), nrows, p->pool,
-                                                                       S->pool, S->stride, S->exps);
+        if (nurows > 0) {
+            slice_r_tb_kernel<kNS><<<(nurows + 127) / 128, 128, 0, st>>>(d_uj, d_ub, (int)uj.size(), nurows,
+                                                                        p->pool, S->pool, S->stride, S->exps);
+            note_launch();
+        }
+        if (nlrows > 0) {
+            slice_r_tb_kernel<kNS><<<(nlrows + 127) / 128, 128, 0, st>>>(d_lj, d_lb, (int)lj.size(), nlrows,
+                                                                        p->pool, S->pool, S->stride, S->exps);
             note_launch();
         }
         cudaError_t e2 = cudaGetLastError();
         if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
         cudaFree(d_vj);
         cudaFree(d_vb);
-        cudaFree(d_rj);
-        cudaFree(d_rb);
+        cudaFree(d_uj);
+        cudaFree(d_ub);
+        cudaFree(d_lj);
+        cudaFree(d_lb);
         if (e2 != cudaSuccess) return fail(DPLR_GPU_ECUDA, "slicing: %s", cudaGetErrorString(e2));
     }
     // schedule: panel items, reduces, 128-row tiles
@@ -1874,6 +1896,9 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
         const int nkb = (L.rank + 15) / 16;
+        // each term keeps its own row and column exponents (one read-out per
+        // term): sharing them across levels costs the residual about 3x in
+        // accuracy on the N = 2^18 kernel matrix
         for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += tc2::M)
             per[t0 / tc2::M].push_back(XTerm{ua[b] + (long long)((t0 - L.row0) / tc2::M) * nkb * kTbA,
                                              A.reduces[ridx[b]].tpad, L.rank, eu_off[b] + (t0 - L.row0), 0, ridx[b]});
@@ -1895,23 +1920,26 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     return tb_attrs<kNS, kD>();
 }
 
+// NSR slices of the stored ones (the residual uses all 8).
+template <int NSR>
 static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int ldx, const double *B, int ldb,
                               double *R, int ldr, cudaStream_t st)
 {
+    constexpr int DR = NSR + 1;
     const int m = p->m;
     const SSchedule &A = S->apply;
     const int njt = (nrhs + 63) / 64;
     int rc;
     {
-        ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * kNS * m * nrhs);
-        if ((rc = slice_x_tb<kNS>(X, m, ldx, nrhs, S->xs, S->xs_elems, S->xexp, S->xexp_n, st))) return rc;
+        ProfScope ps("slice_x", st, 0.0, 8.0 * m * nrhs + 2.0 * NSR * m * nrhs);
+        if ((rc = slice_x_tb<NSR>(X, m, ldx, nrhs, S->xs, S->xs_elems, S->xexp, S->xexp_n, st))) return rc;
     }
     // scratch: partials, DD T, T slices, T exponents (256-byte carves)
     auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t part_bytes = r256((size_t)A.partial_per_rhs * nrhs * sizeof(__int128));
     const size_t t_bytes = r256((size_t)2 * A.t_per_rhs * nrhs * sizeof(double));
     const long long tstride = A.tpre * njt;
-    const size_t ts_bytes = r256((size_t)kNS * tstride * sizeof(bf16));
+    const size_t ts_bytes = r256((size_t)NSR * tstride * sizeof(bf16));
     const size_t te_bytes = r256((size_t)std::max<size_t>(A.reduces.size(), 1) * nrhs * sizeof(int));
     const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes;
     if (S->work_bytes < need) {
@@ -1929,26 +1957,26 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
     bf16 *ts = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes);
     int *texp = reinterpret_cast<int *>(base + part_bytes + t_bytes + ts_bytes);
     int npairs = 0;
-    for (int d = 2; d <= kD; ++d)
-        for (int pp = std::max(1, d - kNS); pp <= std::min(kNS, d - 1); ++pp) ++npairs;
+    for (int d = 2; d <= DR; ++d)
+        for (int pp = std::max(1, d - NSR); pp <= std::min(NSR, d - 1); ++pp) ++npairs;
     if (!A.pitems.empty()) {
         double fl = 0, by = 0;
         for (const PItem &it : A.pitems) {
             fl += 2.0 * it.nkb * 16 * std::min(64, it.rank - it.kt) * nrhs;
-            by += 2.0 * kNS * ((double)it.nkb * 16 * it.nr + (double)it.nkb * 16 * nrhs);
+            by += 2.0 * NSR * ((double)it.nkb * 16 * it.nr + (double)it.nkb * 16 * nrhs);
         }
         {
             ProfScope ps("sliced_panel", st, fl * npairs, by);
-            launch_panel_tb<kNS, kD>(p, A, S->pool, S->stride, S->xs, m, nrhs, partials, st);
+            launch_panel_tb<NSR, DR>(p, A, S->pool, S->stride, S->xs, m, nrhs, partials, st);
             DG_CUDA(cudaGetLastError());
         }
         ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
         const long long maxcnt = (long long)A.max_rank * nrhs;
-        sp_reduce_kernel<kD><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
+        sp_reduce_kernel<DR><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
             A.d_reduces, partials, S->exps, S->xexp, p->pool, nrhs, T, lo_off);
         note_launch();
         const long long warps = (long long)A.reduces.size() * njt * 64;
-        tslice_tb_kernel<kNS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+        tslice_tb_kernel<NSR><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
             A.d_reduces, (int)A.reduces.size(), T, lo_off, nrhs, njt, ts, tstride, texp);
         note_launch();
         DG_CUDA(cudaGetLastError());
@@ -1957,10 +1985,10 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
         double fl = 0, by = 0;
         for (const XTerm &t : A.xterms) {
             fl += 2.0 * tc2::M * t.K * nrhs;
-            by += 2.0 * kNS * ((double)tc2::M * pad16(t.K)) + 2.0 * kNS * pad16(t.K) * nrhs;
+            by += 2.0 * NSR * ((double)tc2::M * pad16(t.K)) + 2.0 * NSR * pad16(t.K) * nrhs;
         }
         ProfScope ps("sliced_expand", st, fl * npairs, by + 16.0 * m * nrhs);
-        launch_expand_tb<kNS, kD>(p, A, S->pool, S->stride, S->exps, ts, tstride, texp, S->xs, m, S->xexp, nrhs,
+        launch_expand_tb<NSR, DR>(p, A, S->pool, S->stride, S->exps, ts, tstride, texp, S->xs, m, S->xexp, nrhs,
                                   true, B, ldb, true, R, ldr, st);
         DG_CUDA(cudaGetLastError());
     }

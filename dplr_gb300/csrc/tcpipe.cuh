@@ -297,6 +297,7 @@ __device__ __forceinline__ void teardown(Ctl &ctl, int warp, int lane, int issue
 // ------------------------------------------------------------- expand
 __device__ __forceinline__ int nkb_of(int K) { return (K + KB - 1) / KB; }
 
+
 // Y[tile, 64 columns] = (-1)^neg sum_terms A_t B_t (+ Bin).  Work item
 // it = tile * njt + jt (right-hand-side tiles of one row tile adjacent).
 // LEAN (D <= 7, every tile a single term, as in the inner solve): the exact
@@ -386,14 +387,28 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * 32);
         int ec = 0;
         if constexpr (LEAN) {
+            // the item's exponents and its 32 values of Bin do not depend on
+            // the products: they are loaded before waiting for the MMAs (and
+            // the next item's exponents before this item's output pass)
+            auto meta = [&](int it, int &re, int &cel, int &nkb) {
+                const int tile = it / njt, jt = it % njt;
+                const XTerm tt = terms[tile_begin[tile]];
+                const int myj = jt * N + ch * 32 + lane;
+                nkb = nkb_of(tt.K);
+                re = aexp[tt.aexp + row] - 7 * D;
+                cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
+            };
+            int re = 0, cel = 0, nkb = 0;
+            if (blockIdx.x < nitems) meta(blockIdx.x, re, cel, nkb);
             for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
                 const int tile = it / njt, jt = it % njt;
-                const int q0 = tile_begin[tile];
-                const int j0 = jt * N + ch * 32, myj = j0 + lane;
-                const XTerm tt = terms[q0];
-                const int nkb = nkb_of(tt.K);
-                const int re = aexp[tt.aexp + row] - 7 * D;
-                const int cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
+                const int j0 = jt * N + ch * 32;
+                const int gr = tile_row0[tile] + row;
+                double bv[32];
+                if (addb) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) bv[c] = j0 + c < nrhs ? Bin[gr + (long long)(j0 + c) * ldbin] : 0.0;
+                }
                 long long acc[32];
 #pragma unroll
                 for (int c = 0; c < 32; ++c) acc[c] = 0;
@@ -417,14 +432,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                     ++ec;
                 }
                 if (!ok) break;
-                const int gr = tile_row0[tile] + row;
+                const int rcur = re, ccur = cel;
+                if (it + (int)gridDim.x < nitems) meta(it + gridDim.x, re, cel, nkb);
 #pragma unroll
                 for (int c = 0; c < 32; ++c) {
                     const int j = j0 + c;
-                    const int ce = __shfl_sync(0xffffffffu, cel, c);
+                    const int ce = __shfl_sync(0xffffffffu, ccur, c);
                     if (j < nrhs) {
-                        const double t = i64_scaled(neg ? -acc[c] : acc[c], re + ce);
-                        Y[gr + (long long)j * ldy] = addb ? Bin[gr + (long long)j * ldbin] + t : t;
+                        const double t = i64_scaled(neg ? -acc[c] : acc[c], rcur + ce);
+                        Y[gr + (long long)j * ldy] = addb ? bv[c] + t : t;
                     }
                 }
             }
