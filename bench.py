@@ -53,8 +53,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="inner solver of the refinement: sliced tensor-core sweep or FP64 sweep")
-    ap.add_argument("--mixed-slices", type=int, default=6,
-                    help="bf16 slices of the mixed inner solve (3 to 6)")
+    ap.add_argument("--mixed-slices", type=int, default=7,
+                    help="bf16 slices of the mixed inner solve (3 to 7)")
     ap.add_argument("--residual", choices=["sliced", "fp64"], default="sliced",
                     help="refinement residual: exact-slice tensor-core products or the FP64 apply")
     ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint"], default="solve",

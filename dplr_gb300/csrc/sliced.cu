@@ -650,38 +650,19 @@ int sliced_error(Plan *p)
     return fail(DPLR_GPU_ECUDA, "tensor-core slice product: a bounded wait expired");
 }
 
-template <int NS, int D>
-static int tc_attrs()
-{
-    using C = tc::Cfg<NS>;
-    DG_CUDA(cudaFuncSetAttribute(tc::tc_panel_kernel<NS, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    DG_CUDA(cudaFuncSetAttribute(tc::tc_expand_kernel<NS, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    return 0;
-}
-
-// Panel launch of a schedule (tcgen05 or mma.sync kernel).
+// Panel launch of a schedule (mma.sync kernel; 16-row tiles).
 template <int NS, int D>
 static void launch_panel(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const bf16 *xs,
                          long long xstride, int ldx, int nrhs, __int128 *partials, cudaStream_t st)
 {
-    if (S.tile_m == tc::M) {
-        const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
-        const unsigned kt = (unsigned)((S.max_rank + tc::M - 1) / tc::M);
-        const unsigned ni = (unsigned)S.items.size();
-        const int on_x = ni > 65535u;
-        tc::tc_panel_kernel<NS, D><<<on_x ? dim3(ni, rt, kt) : dim3(rt, ni, kt), tc::THREADS, tc::Cfg<NS>::SMEM,
-                                     st>>>(S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials, p->tc_err_d,
-                                           on_x);
-    } else {
-        const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
-        sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rt), kSThreads,
-                                     (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
-            S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials);
-    }
+    const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
+    sp_panel_kernel<NS, NS, D><<<dim3((unsigned)S.items.size(), rt), kSThreads,
+                                 (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
+        S.d_items, apool, astride, xs, xstride, ldx, nrhs, partials);
     note_launch();
 }
 
-// Expand launch of a schedule: Y = -/+ sum terms (+ Bin).
+// Expand launch of a schedule: Y = -/+ sum terms (+ Bin) (mma.sync kernel).
 template <int NS, int D>
 static void launch_expand(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
                           const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, long long xstride,
@@ -689,19 +670,10 @@ static void launch_expand(const Plan *p, const SSchedule &S, const bf16 *apool, 
                           double *Y, int ldy, cudaStream_t st)
 {
     const unsigned ntiles = (unsigned)S.tile_row0.size();
-    if (S.tile_m == tc::M) {
-        const unsigned rt = (unsigned)((nrhs + tc::N - 1) / tc::N);
-        const int on_x = ntiles > 65535u;
-        tc::tc_expand_kernel<NS, D><<<on_x ? dim3(ntiles, rt) : dim3(rt, ntiles), tc::THREADS, tc::Cfg<NS>::SMEM,
-                                      st>>>(
-            S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
-            xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d, on_x);
-    } else {
-        const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
-        sp_expand_kernel<NS, NS, D><<<dim3(ntiles, rt), kSThreads, (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
-            S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
-            xexp, nrhs, neg ? -1.0 : 1.0, Bin, ldbin, addb ? 1.0 : 0.0, Y, ldy);
-    }
+    const unsigned rt = (unsigned)((nrhs + ST - 1) / ST);
+    sp_expand_kernel<NS, NS, D><<<dim3(ntiles, rt), kSThreads, (size_t)(2 * NS) * ST * SLD * sizeof(bf16), st>>>(
+        S.d_terms, S.d_tile_row0, S.d_tile_begin, apool, astride, aexp, ts, tstride, texp, xs, xstride, ldx,
+        xexp, nrhs, neg ? -1.0 : 1.0, Bin, ldbin, addb ? 1.0 : 0.0, Y, ldy);
     note_launch();
 }
 
@@ -919,7 +891,7 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
     DG_CUDA(cudaFuncSetAttribute(sp_expand_kernel<kNS, kNS, kD>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(kNS, kNS)));
-    return tc_attrs<kNS, kD>();
+    return 0;
 }
 
 // Scratch of one sliced apply with nrhs columns: X slices, exponents,
@@ -1039,7 +1011,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
 // ====================================================== low-precision solve
 
 // Slice counts of the inner solve: kMSMin..kMSMax slices, pairs p + q <= NS + 1.
-constexpr int kMSMin = 3, kMSMax = 6;
+constexpr int kMSMin = 3, kMSMax = 7;
 
 static int pair_count(int ns, int dmax)
 {
@@ -1113,7 +1085,6 @@ static int mixed_slice_t(const std::vector<SliceJob> &vj, const std::vector<int>
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem(NS, NS));
         if (e3 != cudaSuccess) rc = fail(DPLR_GPU_ECUDA, "mixed solve: %s", cudaGetErrorString(e3));
     }
-    if (!rc) rc = tc_attrs<NS, NS + 1>();
 out:
     cudaFree(d_vj);
     cudaFree(d_vb);
@@ -1142,7 +1113,8 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
         case 3: return mixed_build_tb_t<3>(p, M, F, st);
         case 4: return mixed_build_tb_t<4>(p, M, F, st);
         case 5: return mixed_build_tb_t<5>(p, M, F, st);
-        default: return mixed_build_tb_t<6>(p, M, F, st);
+        case 6: return mixed_build_tb_t<6>(p, M, F, st);
+        default: return mixed_build_tb_t<7>(p, M, F, st);
         }
     }
     const int m = p->m;
@@ -1194,7 +1166,8 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
     case 3: rc = mixed_slice_t<3>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
     case 4: rc = mixed_slice_t<4>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
     case 5: rc = mixed_slice_t<5>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
-    default: rc = mixed_slice_t<6>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    case 6: rc = mixed_slice_t<6>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
+    default: rc = mixed_slice_t<7>(vj, vbase, ncols, zj, lj, p->pool, F->zpool, F->leafinv, M, st); break;
     }
     if (rc) return rc;
 
@@ -1418,14 +1391,16 @@ int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx,
         case 3: return mixed_solve_tb<3>(p, M, F, nrhs, B, ldb, X, ldx, st);
         case 4: return mixed_solve_tb<4>(p, M, F, nrhs, B, ldb, X, ldx, st);
         case 5: return mixed_solve_tb<5>(p, M, F, nrhs, B, ldb, X, ldx, st);
-        default: return mixed_solve_tb<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        case 6: return mixed_solve_tb<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+        default: return mixed_solve_tb<7>(p, M, F, nrhs, B, ldb, X, ldx, st);
         }
     }
     switch (M->ns) {
     case 3: return mixed_solve_t<3>(p, M, F, nrhs, B, ldb, X, ldx, st);
     case 4: return mixed_solve_t<4>(p, M, F, nrhs, B, ldb, X, ldx, st);
     case 5: return mixed_solve_t<5>(p, M, F, nrhs, B, ldb, X, ldx, st);
-    default: return mixed_solve_t<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    case 6: return mixed_solve_t<6>(p, M, F, nrhs, B, ldb, X, ldx, st);
+    default: return mixed_solve_t<7>(p, M, F, nrhs, B, ldb, X, ldx, st);
     }
 }
 
@@ -1730,7 +1705,7 @@ int tb_attrs()
                                  tc2::Cfg<NS>::SMEM));
     DG_CUDA(cudaFuncSetAttribute(tc2::expand_kernel<NS, D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc2::Cfg<NS>::SMEM));
-    if constexpr (D <= 7)
+    if constexpr (D <= 8)
         DG_CUDA(cudaFuncSetAttribute(tc2::expand_kernel<NS, D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      tc2::Cfg<NS>::SMEM));
     return 0;
@@ -1769,7 +1744,7 @@ void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long
     const long long xstride = (long long)(m / 16) * xnjt_of(nrhs) * kTbB;
     bool single = true;                         // every tile one term: the 64-bit epilogue applies
     for (size_t t = 0; t + 1 < S.tile_begin.size(); ++t) single = single && S.tile_begin[t + 1] - S.tile_begin[t] == 1;
-    if constexpr (D <= 7) {
+    if constexpr (D <= 8) {
         if (single) {
             tc2::expand_kernel<NS, D, true><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
                 S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs,

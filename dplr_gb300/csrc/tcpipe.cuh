@@ -1,7 +1,6 @@
 // tcpipe.cuh -- warp-specialised persistent tcgen05 kernels for the
-// exact-slice products (second generation; the arithmetic is the one of
-// tcslice.cuh: one FP32 TMEM accumulator per slice diagonal, exact
-// read-out every 256 inner elements, 128-bit integer combination).
+// exact-slice products: one FP32 TMEM accumulator per slice diagonal, exact
+// read-out every 256 inner elements, 64- or 128-bit integer combination.
 //
 // Operand layout ("tile-blocks"): every slice of every operand is stored as
 // tile-blocks of R rows x 16 inner elements (R = 128 or 64, or the padded
@@ -35,7 +34,6 @@ using tc::commit;
 using tc::fence_after;
 using tc::fence_before;
 using tc::fint;
-using tc::ld8;
 using tc::ld_wait;
 using tc::su32;
 
@@ -140,12 +138,22 @@ __device__ __forceinline__ void read4(uint32_t trow, int c4, __int128 (&W)[4])
     for (int u = 0; u < 4; ++u) W[u] = (DH >= 2 ? ((__int128)ghi[u] << 28) : (__int128)0) + glo[u];
 }
 
-// Same read-out for D <= 7 as one 64-bit integer per column (the exact sum
-// stays below 2^62: six diagonals of |I| < 2^24 shifted by at most 35).
+// Bits the 64-bit read-out drops: for D = 8 it counts in units 2^-7(D-1)
+// and the lowest diagonal is shifted right by 7 (rounded), so every shift
+// stays <= 35 bits.
+template <int D>
+constexpr int kLeanDrop = D > 7 ? 7 * (D - 7) : 0;
+
+// Same read-out for D <= 8 as one 64-bit integer per column, in units
+// 2^(kLeanDrop - 7D).  The sum stays below 2^62: at most seven diagonals of
+// |I| < 2^24 shifted by at most 35.  For D <= 7 it is exact; for D = 8 the
+// dropped 7 bits sit 2^-66 below the leading diagonal, far under the
+// truncation of the slice pairs beyond D.
 template <int D>
 __device__ __forceinline__ void read4_64(uint32_t trow, int c4, long long (&W)[4])
 {
-    static_assert(D <= 7, "64-bit read-out holds at most six diagonals");
+    static_assert(D <= 8, "64-bit read-out holds at most seven diagonals");
+    constexpr int DROP = kLeanDrop<D>;
     uint32_t r[D - 1][4];
 #pragma unroll
     for (int d = 2; d <= D; ++d) ld4(trow + (uint32_t)((d - 2) * N + c4 * 4), r[d - 2]);
@@ -154,7 +162,13 @@ __device__ __forceinline__ void read4_64(uint32_t trow, int c4, long long (&W)[4
     for (int u = 0; u < 4; ++u) {
         long long w = 0;
 #pragma unroll
-        for (int d = 2; d <= D; ++d) w += fint(r[d - 2][u], 7 * (D - d));
+        for (int d = 2; d <= D; ++d) {
+            const int sh = 7 * (D - d) - DROP;
+            if (sh >= 0)
+                w += fint(r[d - 2][u], sh);
+            else
+                w += (fint(r[d - 2][u], 0) + (1LL << (-sh - 1))) >> (-sh);
+        }
         W[u] = w;
     }
 }
@@ -300,9 +314,9 @@ __device__ __forceinline__ int nkb_of(int K) { return (K + KB - 1) / KB; }
 
 // Y[tile, 64 columns] = (-1)^neg sum_terms A_t B_t (+ Bin).  Work item
 // it = tile * njt + jt (right-hand-side tiles of one row tile adjacent).
-// LEAN (D <= 7, every tile a single term, as in the inner solve): the exact
+// LEAN (D <= 8, every tile a single term, as in the inner solve): the
 // product of each output is one 64-bit integer, rounded once to FP64 and
-// added to Bin in FP64 (accurate to the inner solve's 43 bits); otherwise
+// added to Bin in FP64 (accurate far beyond the inner solve's slices); otherwise
 // all terms and Bin meet in a 128-bit fixed-point sum rounded once.
 template <int NS, int D, bool LEAN>
 __global__ void __launch_bounds__(THREADS, 1)
@@ -395,7 +409,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const XTerm tt = terms[tile_begin[tile]];
                 const int myj = jt * N + ch * 32 + lane;
                 nkb = nkb_of(tt.K);
-                re = aexp[tt.aexp + row] - 7 * D;
+                re = aexp[tt.aexp + row] - 7 * D + kLeanDrop<D>;
                 cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
             };
             int re = 0, cel = 0, nkb = 0;

@@ -96,8 +96,8 @@ class GpuPlan:
                                                       ctypes.byref(nb), ctypes.byref(ms)), "dplr_gpu_autotune")
         return {"chunk_rows": c.value, "nb_cap": nb.value, "apply_ms": ms.value}
 
-    def prepare_mixed(self, slices: int = 6, stream=None) -> None:
-        """Sliced factor copies (3 to 6 bf16 slices) for the low-precision inner solve."""
+    def prepare_mixed(self, slices: int = 7, stream=None) -> None:
+        """Sliced factor copies (3 to 7 bf16 slices) for the low-precision inner solve."""
         _native.check(_native.lib().dplr_gpu_prepare_mixed(self._h, int(slices), _stream_ptr(stream)),
                       "dplr_gpu_prepare_mixed")
         self.mixed = True

@@ -89,7 +89,7 @@ DPLR_API int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int l
 
 /* Low-precision inner solver for refinement: the Woodbury sweep with V,
  * the D^-1 W panels and the leaf inverses cut into `slices` bf16 slices
- * (3 to 6: 22 to 43 bits) on the tensor cores, capacitance inverses
+ * (3 to 7: 22 to 50 bits) on the tensor cores, capacitance inverses
  * applied in FP64.  More slices cost more tensor-core work per solve but
  * keep the refinement convergent on worse-conditioned factorisations.
  * Needs dplr_gpu_factor first and leaf sizes that are multiples of 64. */

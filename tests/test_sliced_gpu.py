@@ -155,11 +155,10 @@ def _plan(t, mma: bool, mixed_slices: int = 0):
 @pytest.mark.parametrize("kind", ["random_rank160", "kernel2d"])
 def test_tcgen05_residual_matches_mma_sync(kind):
     """Both kernel families compute exact integer products of 57-bit slices
-    and round once; the tcgen05 path slices U with one exponent per matrix
-    row and T with one per column (shared by a tile's terms, which then
-    accumulate together), so the two agree to the slice-truncation level,
-    about 2^-57 |A||x|.  70 right-hand sides exercise a ragged 64-column
-    tile; ranks above 128 exercise the panel's later rank tiles."""
+    and round once; their operand slicing differs (the tcgen05 path cuts U
+    and T per 128-row tile-block), so the two agree to the slice-truncation
+    level, about 2^-57 |A||x|.  70 right-hand sides exercise a ragged
+    64-column tile; ranks above 128 exercise the panel's later rank tiles."""
     from dplr_gb300 import gen_gpu
     if kind == "kernel2d":
         t = gen_gpu.kernel_tree_2d(n=8192, leaf=128, rmax=96, seed=8)
@@ -185,14 +184,16 @@ def test_tcgen05_residual_matches_mma_sync(kind):
     assert float(np.linalg.norm(rt - rm)) / nax <= 2e-15
 
 
-def test_tcgen05_mixed_refined_solve():
+@pytest.mark.parametrize("ns", [6, 7])
+def test_tcgen05_mixed_refined_solve(ns):
     """Mixed refinement with the tcgen05 kernels reaches the tolerance and
-    agrees with the mma.sync path's solution."""
+    agrees with the mma.sync path's solution (7 slices: 8 diagonals, whose
+    64-bit read-out drops 7 bits of the lowest one)."""
     from dplr_gb300 import gen_gpu
     t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, rmax=96, seed=6)
     g = torch.Generator(device="cpu").manual_seed(2)
     b = torch.randn(70, t.size, generator=g, dtype=torch.float64).cuda()
-    pt, pm = _plan(t, mma=False, mixed_slices=6), _plan(t, mma=True, mixed_slices=6)
+    pt, pm = _plan(t, mma=False, mixed_slices=ns), _plan(t, mma=True, mixed_slices=ns)
     xt, rt, _ = pt.solve_refined(b, tol=1e-12, maxiter=10, precise=True, mixed=True)
     xm, rm, _ = pm.solve_refined(b, tol=1e-12, maxiter=10, precise=True, mixed=True)
     pt.close()
@@ -200,3 +201,19 @@ def test_tcgen05_mixed_refined_solve():
     assert rt <= 1e-12 and rm <= 1e-12, (rt, rm)
     rel = float(((xt - xm).norm(dim=1) / xm.norm(dim=1)).max())
     assert rel <= 1e-9, rel
+
+
+def test_seventh_slice_shrinks_inner_solve_error():
+    """One unrefined mixed solve: each slice adds 7 bits, so 7 slices leave
+    a residual about two orders of magnitude below 6 (the diagnostics on
+    this matrix give ratios of about 100 per slice)."""
+    from dplr_gb300 import gen_gpu
+    t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, rmax=96, seed=6)
+    g = torch.Generator(device="cpu").manual_seed(3)
+    b = torch.randn(16, t.size, generator=g, dtype=torch.float64).cuda()
+    res = {}
+    for ns in (5, 6, 7):
+        p = _plan(t, mma=False, mixed_slices=ns)
+        _, res[ns], _ = p.solve_refined(b, tol=1e-30, maxiter=0, precise=True, mixed=True, strict=False)
+        p.close()
+    assert res[6] < res[5] / 20 and res[7] < res[6] / 20, res
