@@ -690,8 +690,10 @@ static void free_sschedule(SSchedule &A)
 {
     cudaFree(A.d_pitems);
     cudaFree(A.d_xterms);
+    cudaFree(A.d_rmax);
     A.d_pitems = nullptr;
     A.d_xterms = nullptr;
+    A.d_rmax = nullptr;
     cudaFree(A.d_items);
     cudaFree(A.d_reduces);
     cudaFree(A.d_tile_row0);
@@ -1596,6 +1598,34 @@ __global__ void tslice_tb_kernel(const SReduceItem *__restrict__ items, int nite
     }
 }
 
+// Alignment exponents of the multi-term expand: per tile row the largest
+// row exponent of the tile's terms (fixed once the factors are sliced), and
+// per tile and right-hand side the largest column exponent (T or X slices,
+// per call).  Empty tiles and columns get 0, as the kernel expects.
+__global__ void tile_rmax_kernel(const XTerm *__restrict__ terms, const int *__restrict__ tile_begin, int ntiles,
+                                 const int *__restrict__ aexp, int *__restrict__ rmax)
+{
+    const int tile = blockIdx.x, row = threadIdx.x;
+    if (tile >= ntiles) return;
+    int r = -100000;
+    for (int q = tile_begin[tile]; q < tile_begin[tile + 1]; ++q) r = max(r, aexp[terms[q].aexp + row]);
+    rmax[(long long)tile * tc2::M + row] = r < -99999 ? 0 : r;
+}
+
+__global__ void tile_cmax_kernel(const XTerm *__restrict__ terms, const int *__restrict__ tile_begin, int ntiles,
+                                 const int *__restrict__ texp, const int *__restrict__ xexp, int nrhs,
+                                 int *__restrict__ cmax)
+{
+    const int tile = blockIdx.x, j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (tile >= ntiles || j >= nrhs) return;
+    int c = -100000;
+    for (int q = tile_begin[tile]; q < tile_begin[tile + 1]; ++q) {
+        const XTerm tt = terms[q];
+        c = max(c, tt.src == 0 ? texp[(long long)tt.blk * nrhs + j] : xexp[j]);
+    }
+    cmax[(long long)tile * nrhs + j] = c < -99999 ? 0 : c;
+}
+
 int upload_tb(SSchedule &S, long long *bytes)
 {
     int rc;
@@ -1736,7 +1766,7 @@ template <int NS, int D>
 void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
                       const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, int m, const int *xexp,
                       int nrhs, bool neg, const double *Bin, int ldbin, bool addb, double *Y, int ldy,
-                      cudaStream_t st)
+                      cudaStream_t st, const int *rmaxt = nullptr, const int *cmaxt = nullptr)
 {
     const int njt = (nrhs + 63) / 64;
     const int nt = (int)S.tile_row0.size();
@@ -1748,14 +1778,15 @@ void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long
         if (single) {
             tc2::expand_kernel<NS, D, true><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
                 S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs,
-                xstride, xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+                xstride, xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, nullptr, nullptr,
+                p->tc_err_d);
             note_launch();
             return;
         }
     }
     tc2::expand_kernel<NS, D, false><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
         S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs, xstride,
-        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, p->tc_err_d);
+        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, rmaxt, cmaxt, p->tc_err_d);
     note_launch();
 }
 
@@ -1891,6 +1922,13 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     }
     A.tile_begin.push_back((int)A.xterms.size());
     if ((rc = upload_tb(A, &S->bytes))) return rc;
+    if (ntiles > 0) {
+        DG_CUDA(cudaMalloc((void **)&A.d_rmax, (size_t)ntiles * tc2::M * sizeof(int)));
+        S->bytes += (long long)ntiles * tc2::M * sizeof(int);
+        tile_rmax_kernel<<<ntiles, tc2::M, 0, st>>>(A.d_xterms, A.d_tile_begin, ntiles, S->exps, A.d_rmax);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
     if ((rc = ensure_err_flag(p))) return rc;
     return tb_attrs<kNS, kD>();
 }
@@ -1916,7 +1954,9 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
     const long long tstride = A.tpre * njt;
     const size_t ts_bytes = r256((size_t)NSR * tstride * sizeof(bf16));
     const size_t te_bytes = r256((size_t)std::max<size_t>(A.reduces.size(), 1) * nrhs * sizeof(int));
-    const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes;
+    const int ntiles = (int)A.tile_row0.size();
+    const size_t cm_bytes = r256((size_t)std::max(ntiles, 1) * nrhs * sizeof(int));
+    const size_t need = part_bytes + t_bytes + ts_bytes + te_bytes + cm_bytes;
     if (S->work_bytes < need) {
         cudaFree(S->work);
         S->work = nullptr;
@@ -1931,6 +1971,7 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
     const long long lo_off = A.t_per_rhs * nrhs;
     bf16 *ts = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes);
     int *texp = reinterpret_cast<int *>(base + part_bytes + t_bytes + ts_bytes);
+    int *cmax = reinterpret_cast<int *>(base + part_bytes + t_bytes + ts_bytes + te_bytes);
     int npairs = 0;
     for (int d = 2; d <= DR; ++d)
         for (int pp = std::max(1, d - NSR); pp <= std::min(NSR, d - 1); ++pp) ++npairs;
@@ -1963,8 +2004,11 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
             by += 2.0 * NSR * ((double)tc2::M * pad16(t.K)) + 2.0 * NSR * pad16(t.K) * nrhs;
         }
         ProfScope ps("sliced_expand", st, fl * npairs, by + 16.0 * m * nrhs);
+        tile_cmax_kernel<<<dim3((unsigned)ntiles, (unsigned)((nrhs + 127) / 128)), 128, 0, st>>>(
+            A.d_xterms, A.d_tile_begin, ntiles, texp, S->xexp, nrhs, cmax);
+        note_launch();
         launch_expand_tb<NSR, DR>(p, A, S->pool, S->stride, S->exps, ts, tstride, texp, S->xs, m, S->xexp, nrhs,
-                                  true, B, ldb, true, R, ldr, st);
+                                  true, B, ldb, true, R, ldr, st, A.d_rmax, cmax);
         DG_CUDA(cudaGetLastError());
     }
     return 0;

@@ -85,6 +85,7 @@ struct SSchedule {
     long long tpre = 0;             // T tile-block elements of all blocks per 64-column rhs tile
     PItem *d_pitems = nullptr;
     XTerm *d_xterms = nullptr;
+    int *d_rmax = nullptr;          // per tile row: max row exponent of the tile's terms (static)
     std::vector<SPanelItem> items;
     std::vector<SReduceItem> reduces;
     long long partial_per_rhs = 0;

@@ -248,20 +248,37 @@ __device__ __forceinline__ void wait_raw(uint64_t *bar, uint32_t parity)
 }
 
 // All slice pairs p + q <= D of one stage (A: NS blocks of 128 rows, B: NS
-// blocks of `nb` rows), diagonal d into TMEM columns (d - 2) * 64.
-template <int NS, int D>
-__device__ __forceinline__ void issue(uint32_t tmem, uint32_t a0, uint32_t b0, int nb, uint32_t idesc, bool first)
+// blocks of `nb` rows), diagonal d into TMEM columns (d - 2) * 64.  The
+// slices of a stage sit at fixed distances, so every descriptor is the
+// stage's base descriptor plus a multiple of the distance / 16 (the 14-bit
+// address field cannot carry: shared addresses are below 256 KB); fully
+// unrolled, one MMA costs the issuing thread a few instructions.  FIRST
+// starts each diagonal's accumulation.
+template <int NS, int D, bool FIRST>
+__device__ __forceinline__ void issue(uint32_t tmem, uint64_t ad0, uint64_t bd0, uint32_t bstep, uint32_t idesc)
 {
-#pragma unroll 1
-    for (int d = 2; d <= D; ++d) {
-        const int plo = d - NS > 1 ? d - NS : 1, phi = d - 1 < NS ? d - 1 : NS;
 #pragma unroll
-        for (int p = plo; p <= phi; ++p) {
-            const uint64_t ad = sdesc(a0 + (uint32_t)((p - 1) * TB_A * 2));
-            const uint64_t bd = sdesc(b0 + (uint32_t)((d - p - 1) * nb * KB * 2));
-            mma_n(tmem + (uint32_t)((d - 2) * N), ad, bd, idesc, (first && p == plo) ? 0u : 1u);
+    for (int d = 2; d <= D; ++d) {
+#pragma unroll
+        for (int p = 1; p <= NS; ++p) {
+            const int q = d - p;
+            if (q < 1 || q > NS) continue;
+            const bool start = FIRST && p == (d - NS > 1 ? d - NS : 1);
+            mma_n(tmem + (uint32_t)((d - 2) * N), ad0 + (uint64_t)((p - 1) * (TB_A * 2 / 16)),
+                  bd0 + (uint64_t)(q - 1) * bstep, idesc, start ? 0u : 1u);
         }
     }
+}
+
+template <int NS, int D>
+__device__ __forceinline__ void issue_stage(uint32_t tmem, uint32_t a0, int nb, uint32_t idesc, bool first)
+{
+    const uint64_t ad0 = sdesc(a0), bd0 = sdesc(a0 + NS * TB_A * 2);
+    const uint32_t bstep = (uint32_t)(nb * KB * 2 / 16);
+    if (first)
+        issue<NS, D, true>(tmem, ad0, bd0, bstep, idesc);
+    else
+        issue<NS, D, false>(tmem, ad0, bd0, bstep, idesc);
 }
 
 template <int NS, int D>
@@ -325,7 +342,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                   long long astride, const int *__restrict__ aexp, const bf16 *__restrict__ ts, long long tstride,
                   const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int xnjt,
                   const int *__restrict__ xexp, int nrhs, int neg, const double *__restrict__ Bin, int ldbin,
-                  int addb, double *__restrict__ Y, int ldy, int *err)
+                  int addb, double *__restrict__ Y, int ldy, const int *__restrict__ rmaxt,
+                  const int *__restrict__ cmaxt, int *err)
 {
     using C = Cfg<NS>;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -383,7 +401,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             if (!wait_bar(ctl, &ctl.full[s], (uint32_t)((consumed / C::NST) & 1))) break;
                             fence_after();
                             const uint32_t a0 = sbase + (uint32_t)(s * C::STAGE);
-                            issue<NS, D>(tmem, a0, a0 + NS * TB_A * 2, N, idesc, kb == kb0);
+                            issue_stage<NS, D>(tmem, a0, N, idesc, kb == kb0);
                             commit(&ctl.empty[s]);
                             ++consumed;
                         }
@@ -464,24 +482,38 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int q0 = tile_begin[tile], q1 = tile_begin[tile + 1];
             const int j0 = jt * N + ch * 32;         // this warp's first column
             const int myj = j0 + lane;               // column whose exponents this lane holds
-            int rmax = -100000, cmaxl = -100000;
-            for (int q = q0; q < q1; ++q) {
-                const XTerm &tt = terms[q];
-                rmax = max(rmax, aexp[tt.aexp + row]);
-                if (myj < nrhs) cmaxl = max(cmaxl, tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]);
+            // alignment exponents: the tile's largest row exponent per row and
+            // column exponent per column (precomputed, or from the terms)
+            int rmax, cmaxl;
+            if (rmaxt) {
+                rmax = rmaxt[(long long)tile * M + row];
+                cmaxl = myj < nrhs ? cmaxt[(long long)tile * nrhs + myj] : 0;
+            } else {
+                rmax = cmaxl = -100000;
+                for (int q = q0; q < q1; ++q) {
+                    const XTerm &tt = terms[q];
+                    rmax = max(rmax, aexp[tt.aexp + row]);
+                    if (myj < nrhs) cmaxl = max(cmaxl, tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]);
+                }
+                if (rmax < -99999) rmax = 0;
+                if (cmaxl < -99999) cmaxl = 0;
             }
-            if (rmax < -99999) rmax = 0;
-            if (cmaxl < -99999) cmaxl = 0;
             __int128 acc[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) acc[c] = 0;
             bool ok = true;
-            for (int q = q0; q < q1 && ok; ++q) {
+            // a term's shifts and depth, loaded one term ahead of its read-out
+            auto shifts = [&](int q, int &rd, int &cd, int &kbs) {
                 const XTerm tt = terms[q];
-                const int nkb = nkb_of(tt.K);
-                const int rdel = aexp[tt.aexp + row] - rmax + 109 - 7 * D;
-                const int cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
-                const int cdl = cel - cmaxl;         // this lane's column shift part
+                kbs = nkb_of(tt.K);
+                rd = aexp[tt.aexp + row] - rmax + 109 - 7 * D;
+                cd = (myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0) - cmaxl;
+            };
+            int rdel = 0, cdl = 0, nkb = 0;
+            if (q0 < q1) shifts(q0, rdel, cdl, nkb);
+            for (int q = q0; q < q1 && ok; ++q) {
+                int rdn = 0, cdn = 0, nkbn = 0;
+                if (q + 1 < q1) shifts(q + 1, rdn, cdn, nkbn);
                 for (int kb0 = 0; kb0 < nkb; kb0 += RANGE) {
                     if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
                         ok = false;
@@ -503,6 +535,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (lane == 0) arrive(&ctl.acce);
                     ++ec;
                 }
+                rdel = rdn;
+                cdl = cdn;
+                nkb = nkbn;
             }
             if (!ok) break;
             // outputs: fold in +-Bin exactly, round once
@@ -598,7 +633,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (!wait_bar(ctl, &ctl.full[s], (uint32_t)((consumed / C::NST) & 1))) break;
                         fence_after();
                         const uint32_t a0 = sbase + (uint32_t)(s * C::STAGE);
-                        issue<NS, D>(tmem, a0, a0 + NS * TB_A * 2, itm.nr, idesc, kb == kb0);
+                        issue_stage<NS, D>(tmem, a0, itm.nr, idesc, kb == kb0);
                         commit(&ctl.empty[s]);
                         ++consumed;
                     }
