@@ -48,6 +48,7 @@ def _bind(lib: ctypes.CDLL) -> None:
                                           POINTER(c_int), c_void_p])
     sig("dplr_gpu_prepare_sliced", c_int, [c_void_p, c_void_p])
     sig("dplr_gpu_prepare_mixed", c_int, [c_void_p, c_int, c_void_p])
+    sig("dplr_gpu_prepare_pairs", c_int, [c_void_p, c_void_p])
     sig("dplr_gpu_residual", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                      c_int, c_int, c_void_p])
     sig("dplr_gpu_solve_refined_host", c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,

@@ -137,7 +137,13 @@ long long dplr_gpu_plan_device_bytes(dplr_gpu_plan plan)
     Plan *p = (Plan *)plan;
     if (!p) return 0;
     return p->device_bytes + (long long)p->work_doubles * 8 + (long long)p->xbuf_doubles * 8 +
-           (long long)p->ybuf_doubles * 8;
+           (long long)p->ybuf_doubles * 8 + pairs_bytes(p);
+}
+
+int dplr_gpu_prepare_pairs(dplr_gpu_plan plan, void *stream)
+{
+    if (!plan) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_pairs: null plan");
+    return pairs_prepare((Plan *)plan, (cudaStream_t)stream);
 }
 
 int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha, const double *X, int ldx,

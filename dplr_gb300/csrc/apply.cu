@@ -565,6 +565,7 @@ int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, in
         if (!rc && alpha0_squares_beta && beta != 0.0) rc = scale_device(Y, p->m, nrhs, ldy, beta, st);
         return rc;
     }
+    if (pairs_usable(p, trans, nrhs)) return pairs_apply(p, alpha, X, beta, Y, st);
     const Schedule &S = p->sched[trans ? 1 : 0];
     size_t need = (size_t)(S.t_per_rhs + S.partial_per_rhs) * nrhs;
     int rc = ensure_buffer(&p->work, &p->work_doubles, need);

@@ -250,7 +250,7 @@ int dplr_gpu_pool_write(dplr_gpu_plan plan, const double *src, void *stream)
     plan_values_changed(p);
     DG_CUDA(cudaMemcpyAsync(p->pool, src, (size_t)p->pool_doubles * sizeof(double), cudaMemcpyDeviceToDevice,
                             (cudaStream_t)stream));
-    return 0;
+    return pairs_refresh(p, (cudaStream_t)stream);    // the pair copy follows the new values
 }
 
 int dplr_gpu_grad_factors(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *DY, int ldy,

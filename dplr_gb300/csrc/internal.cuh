@@ -157,6 +157,8 @@ struct Plan {
     void *mixed = nullptr;
     // error flag of the tensor-core kernels (mapped host memory, sliced.cu)
     int *tc_err_h = nullptr, *tc_err_d = nullptr;
+    // float-pair copy of the factors for the 1-RHS apply (pairs.cu)
+    void *pairs = nullptr;
     // factor gradients (grad.cu): work lists and scratch
     void *grad = nullptr;
     double *gbuf = nullptr;
@@ -174,6 +176,8 @@ int validate_tree(int m, const DPlrMtx *A, const char *fn);
 
 // schedule helpers (plan.cu)
 int tile_rows_for(const Plan *p);
+void build_tiles(const Plan *p, int trans, int R, std::vector<int> &row0, std::vector<int> &begin,
+                 std::vector<TileTerm> &terms);
 int upload_schedule(Schedule &S, long long *bytes);
 void free_schedule(Schedule &S);
 
@@ -189,6 +193,14 @@ int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int 
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,
                  double beta, double *Y, int ldy, cudaStream_t st, bool alpha0_squares_beta);
 int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream_t st);
+
+// pairs.cu: FP64-accurate 1-RHS apply on the FP32 pipes
+int pairs_prepare(Plan *p, cudaStream_t st);
+int pairs_refresh(Plan *p, cudaStream_t st);
+void pairs_free(Plan *p);
+bool pairs_usable(const Plan *p, int trans, int nrhs);
+int pairs_apply(Plan *p, double alpha, const double *X, double beta, double *Y, cudaStream_t st);
+long long pairs_bytes(const Plan *p);
 
 // grad.cu
 void grad_free(Plan *p);

@@ -122,7 +122,7 @@ struct Builder {
             d.toff = p->total_rank;
             p->total_rank += d.rank;
             p->max_rank = std::max(p->max_rank, d.rank);
-            p->nnz += (long long)h * d.rank;
+            p->nnz += 2LL * h * d.rank;          // U and V, as src/dplrnz.c:45 counts
             ids[s] = (int)p->lr.size();
             p->lr.push_back(d);
         }
@@ -158,43 +158,11 @@ int tile_rows_for(const Plan *p)
 // Apply schedule for op N (trans = 0) or op T (trans = 1): panels contract
 // V (U) with x over the block's input rows, tiles expand U (V) T_b over the
 // block's output rows plus the leaf term.
-static void build_schedule(Plan *p, int trans, Schedule &S)
+// Output tiles of R rows (R divides every leaf) and their terms: every
+// low-rank block whose output rows cover the tile, then the leaf term.
+void build_tiles(const Plan *p, int trans, int R, std::vector<int> &row0, std::vector<int> &begin,
+                 std::vector<TileTerm> &terms)
 {
-    const int CH = p->chunk_rows;
-    S.items.clear();
-    S.reduces.clear();
-    long long poff = 0;
-    for (size_t b = 0; b < p->lr.size(); ++b) {
-        const LRDesc &L = p->lr[b];
-        if (L.rank == 0 || L.n == 0) continue;
-        int nch = (L.n + CH - 1) / CH;
-        for (int c = 0; c < nch; ++c) {
-            PanelItem it;
-            it.f = trans ? L.u : L.v;
-            it.p = poff;
-            it.in0 = trans ? L.row0 : L.col0;
-            it.n = L.n;
-            it.rank = L.rank;
-            it.r0 = c * CH;
-            it.len = std::min(CH, L.n - c * CH);
-            it.chunk = c;
-            S.items.push_back(it);
-        }
-        ReduceItem r;
-        r.p = poff;
-        r.t = L.toff;
-        r.sig = L.sig;
-        r.rank = L.rank;
-        r.nch = nch;
-        S.reduces.push_back(r);
-        poff += (long long)nch * L.rank;
-    }
-    S.partial_per_rhs = poff;
-    S.t_per_rhs = p->total_rank;
-    S.max_rank = p->max_rank;
-
-    const int R = tile_rows_for(p);
-    S.tile_rows = R;
     int ntiles = p->m / R;
     std::vector<std::vector<TileTerm>> per(ntiles);
     for (size_t b = 0; b < p->lr.size(); ++b) {
@@ -234,15 +202,54 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
             per[t0 / R].push_back(tt);
         }
     }
-    S.tile_row0.clear();
-    S.tile_begin.clear();
-    S.terms.clear();
+    row0.clear();
+    begin.clear();
+    terms.clear();
     for (int t = 0; t < ntiles; ++t) {
-        S.tile_row0.push_back(t * R);
-        S.tile_begin.push_back((int)S.terms.size());
-        S.terms.insert(S.terms.end(), per[t].begin(), per[t].end());
+        row0.push_back(t * R);
+        begin.push_back((int)terms.size());
+        terms.insert(terms.end(), per[t].begin(), per[t].end());
     }
-    S.tile_begin.push_back((int)S.terms.size());
+    begin.push_back((int)terms.size());
+}
+
+static void build_schedule(Plan *p, int trans, Schedule &S)
+{
+    const int CH = p->chunk_rows;
+    S.items.clear();
+    S.reduces.clear();
+    long long poff = 0;
+    for (size_t b = 0; b < p->lr.size(); ++b) {
+        const LRDesc &L = p->lr[b];
+        if (L.rank == 0 || L.n == 0) continue;
+        int nch = (L.n + CH - 1) / CH;
+        for (int c = 0; c < nch; ++c) {
+            PanelItem it;
+            it.f = trans ? L.u : L.v;
+            it.p = poff;
+            it.in0 = trans ? L.row0 : L.col0;
+            it.n = L.n;
+            it.rank = L.rank;
+            it.r0 = c * CH;
+            it.len = std::min(CH, L.n - c * CH);
+            it.chunk = c;
+            S.items.push_back(it);
+        }
+        ReduceItem r;
+        r.p = poff;
+        r.t = L.toff;
+        r.sig = L.sig;
+        r.rank = L.rank;
+        r.nch = nch;
+        S.reduces.push_back(r);
+        poff += (long long)nch * L.rank;
+    }
+    S.partial_per_rhs = poff;
+    S.t_per_rhs = p->total_rank;
+    S.max_rank = p->max_rank;
+
+    S.tile_rows = tile_rows_for(p);
+    build_tiles(p, trans, S.tile_rows, S.tile_row0, S.tile_begin, S.terms);
 }
 
 template <class T>
@@ -317,6 +324,7 @@ int plan_upload_values(Plan *p, const DPlrMtx *A, cudaStream_t st)
     if (rc) return rc;
     if (up.lr_i != p->lr.size() || up.leaf_i != p->leaves.size())
         return fail(DPLR_GPU_EINVAL, "plan refresh: structure changed");
+    if ((rc = pairs_refresh(p, st))) return rc;
     DG_CUDA(cudaStreamSynchronize(st));
     return 0;
 }
@@ -418,6 +426,7 @@ void plan_free(Plan *p)
     mixed_free(p);
     factor_free(p);
     sliced_free(p);
+    pairs_free(p);
     cudaFree(p->pool);
     cudaFree(p->d_lr);
     cudaFree(p->d_leaves);

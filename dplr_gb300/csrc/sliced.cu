@@ -309,14 +309,22 @@ __global__ void xcol_init_kernel(int *xexp, int nrhs)
     if (j < nrhs) xexp[j] = kNoExp;
 }
 
-__global__ void xcol_exp_kernel(const double *X, int m, int ldx, int *xexp)
+__global__ void xcol_exp_kernel(const double *__restrict__ X, int m, int ldx, int *xexp)
 {
     __shared__ double red[256];
     const double *col = X + (long long)blockIdx.x * ldx;
     const int per = (m + gridDim.y - 1) / gridDim.y;
     const int r0 = blockIdx.y * per, r1 = min(m, r0 + per);
     double v = 0.0;
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) v = fmax(v, fabs(col[i]));
+    int i = r0 + threadIdx.x;
+    for (; i + 7 * 256 < r1; i += 8 * 256) {        // 8 independent loads in flight
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = col[i + u * 256];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v = fmax(v, fabs(x[u]));
+    }
+    for (; i < r1; i += 256) v = fmax(v, fabs(col[i]));
     red[threadIdx.x] = v;
     __syncthreads();
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
@@ -1508,55 +1516,62 @@ __global__ void slice_r_tb_kernel(const RSliceJob *jobs, const int *row_base, in
     }
 }
 
-// Pack the NS slices of 8 consecutive values into one 16-byte store per slice.
+// Pack the NS slices of 8 consecutive values into one 16-byte store per
+// slice.  The balanced base-128 digits come out least significant first, so
+// each slice is stored as soon as its 8 digits are known (only the 8 running
+// values stay live).
 template <int NS>
-__device__ __forceinline__ void store8(const long long (&y)[8], bf16 *out, long long stride)
+__device__ __forceinline__ void store8(long long (&v)[8], bf16 *out, long long stride)
 {
-    int a[8][NS];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        long long v = y[u];
+    for (int p = NS - 1; p >= 0; --p) {
+        uint32_t b[8];
 #pragma unroll
-        for (int p = NS - 1; p >= 1; --p) {
-            const long long d = ((v + 64) & 127) - 64;
-            a[u][p] = (int)d;
-            v = (v - d) >> 7;
+        for (int u = 0; u < 8; ++u) {
+            int a;
+            if (p > 0) {
+                const long long d = ((v[u] + 64) & 127) - 64;
+                a = (int)d;
+                v[u] = (v[u] - d) >> 7;
+            } else {
+                a = (int)v[u];
+            }
+            b[u] = digit_bits(a);
         }
-        a[u][0] = (int)v;
-    }
-#pragma unroll
-    for (int p = 0; p < NS; ++p) {
         uint4 w;
-        w.x = digit_bits(a[0][p]) | (digit_bits(a[1][p]) << 16);
-        w.y = digit_bits(a[2][p]) | (digit_bits(a[3][p]) << 16);
-        w.z = digit_bits(a[4][p]) | (digit_bits(a[5][p]) << 16);
-        w.w = digit_bits(a[6][p]) | (digit_bits(a[7][p]) << 16);
+        w.x = b[0] | (b[1] << 16);
+        w.y = b[2] | (b[3] << 16);
+        w.z = b[4] | (b[5] << 16);
+        w.w = b[6] | (b[7] << 16);
         *reinterpret_cast<uint4 *>(out + p * stride) = w;
     }
 }
 
 // X (m x nrhs) into 16-row x 64-column tile-blocks; one thread per
-// (column j, row-block rb), j fastest; columns >= nrhs are zero.
+// (column j, 8-row half h of row-block rb), j fastest, all 8 loads issued
+// before any use; columns >= nrhs are zero.
 template <int NS>
-__global__ void xslice_tb_kernel(const double *X, int m, int ldx, int nrhs, int xnjt, const int *xexp, bf16 *xs,
-                                 long long stride)
+__global__ void xslice_tb_kernel(const double *__restrict__ X, int m, int ldx, int nrhs, int xnjt,
+                                 const int *__restrict__ xexp, bf16 *__restrict__ xs, long long stride)
 {
     const int nrb = m >> 4, ncol = xnjt * 64;
-    const long long cnt = (long long)nrb * ncol;
+    const long long cnt = (long long)nrb * 2 * ncol;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
          t += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(t % ncol), rb = (int)(t / ncol);
+        const int j = (int)(t % ncol);
+        const long long q = t / ncol;
+        const int h = (int)(q & 1), rb = (int)(q >> 1);
         const bool live = j < nrhs;
         const int sh = live ? 7 * NS - xexp[j] : 0;
-        const double *col = X + (long long)(live ? j : 0) * ldx + rb * 16;
-        bf16 *out = xs + ((long long)rb * xnjt + (j >> 6)) * kTbB + tc2::tbo(j & 63, 0);
+        const double *col = X + (long long)(live ? j : 0) * ldx + rb * 16 + h * 8;
+        bf16 *out = xs + ((long long)rb * xnjt + (j >> 6)) * kTbB + tc2::tbo(j & 63, 0) + h * 64;
+        double x[8];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            long long y[8];
+        for (int u = 0; u < 8; ++u) x[u] = live ? col[u] : 0.0;
+        long long y[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) y[u] = live ? scaled_int(col[h * 8 + u], sh) : 0;
-            store8<NS>(y, out + h * 64, stride);
-        }
+        for (int u = 0; u < 8; ++u) y[u] = scaled_int(x[u], sh);
+        store8<NS>(y, out, stride);
     }
 }
 
@@ -1720,8 +1735,8 @@ int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_
         xexp_n = nrhs;
     }
     xcol_exps(X, m, ldx, nrhs, xexp, st);
-    const long long cnt = (long long)(m / 16) * xnjt * 64;
-    const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 16);
+    const long long cnt = (long long)(m / 16) * 2 * xnjt * 64;
+    const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
     xslice_tb_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
     note_launch();
     DG_CUDA(cudaGetLastError());

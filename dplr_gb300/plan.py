@@ -58,6 +58,7 @@ class GpuPlan:
         self.factored_transposed = False
         self.sliced = False
         self.mixed = False
+        self.pairs = False
 
     RESIDUAL_SLICED = 1
     SOLVE_MIXED = 2
@@ -102,6 +103,12 @@ class GpuPlan:
                       "dplr_gpu_prepare_mixed")
         self.mixed = True
         self.mixed_slices = int(slices)
+
+    def prepare_pairs(self, stream=None) -> None:
+        """Float-pair copy of the factors: 1-RHS op-N applies then run on the
+        FP32 pipes (FP64-accurate, compensated sums) at HBM speed."""
+        _native.check(_native.lib().dplr_gpu_prepare_pairs(self._h, _stream_ptr(stream)), "dplr_gpu_prepare_pairs")
+        self.pairs = True
 
     def prepare_sliced(self, stream=None) -> None:
         """Exact-slice factor copies for the precise (tensor-core) residual."""

@@ -59,6 +59,18 @@ DPLR_API long long dplr_gpu_plan_device_bytes(dplr_gpu_plan plan);
 DPLR_API int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha, const double *X,
                    int ldx, double beta, double *Y, int ldy, void *stream);
 
+/* FP64-accurate single-right-hand-side apply on the FP32 pipes.  Keeps a
+ * second copy of the factors as float pairs (hi + lo: the leading 48 bits of
+ * each double, 8 bytes per element); afterwards every op-N apply with one
+ * right-hand side (dplr_gpu_apply, the drop-in dplrgepmv on a registered
+ * plan) evaluates the products with error-free FP32 transformations and
+ * compensated sums (relative error ~1e-14 of |A||x|), streaming the factors
+ * at HBM speed instead of FP64-FMA speed.  Other applies keep the FP64
+ * kernels.  The copy follows dplr_gpu_plan_refresh and dplr_gpu_pool_write
+ * and is freed with the plan.  DPLR_GPU_EINVAL if the largest factor entry
+ * is outside 2^+-50 (FP32 range). */
+DPLR_API int dplr_gpu_prepare_pairs(dplr_gpu_plan plan, void *stream);
+
 /* Woodbury factorisation of the planned matrix (replaces forming inv(A)
  * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):
  * leaf inverses, per-level panels Z = D^-1 W and capacitance inverses

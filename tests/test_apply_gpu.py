@@ -171,3 +171,14 @@ def test_invalid_arguments_leave_output_untouched(gpu, capfd):
     assert np.array_equal(c, np.arange(m * 2, dtype=float))
     err = capfd.readouterr().err
     assert "dplrgepmv: invalid A size" in err and "dplrgepdmm: invalid leading dimensions" in err
+
+
+@pytest.mark.parametrize("name", list(TREES))
+def test_plan_nnz_matches_dplrnz(name):
+    """plan_info's nnz is DPLR's dplrnz: size * (rank_ne + rank_sw) per H node
+    plus the leaves (src/dplrnz.c:17-62)."""
+    from dplr_gb300.plan import GpuPlan
+    t = TREES[name]()
+    p = GpuPlan(t)
+    assert p.nnz == tree.nnz(t)
+    p.close()
