@@ -35,6 +35,10 @@ _SIGNATURES = {
                      c_double_p, c_int, PDPlrMtx, c_double]),
     "geinv": (None, [c_int, PDPlrMtx, PDPlrMtx, c_double, POINTER(c_int)]),
     "reduce": (None, [c_int, PDPlrMtx, c_double]),
+    "cpy": (None, [c_int, PDPlrMtx, PDPlrMtx]),
+    "scal": (None, [c_int, POINTER(c_double), PDPlrMtx]),
+    "axpy": (None, [c_int, POINTER(c_double), PDPlrMtx, PDPlrMtx]),
+    "adpy": (None, [c_int, POINTER(c_double), c_double_p, PDPlrMtx]),
 }
 
 
@@ -101,3 +105,16 @@ class PlrApi:
 
     def reduce(self, m: int, a, eps: float) -> None:
         self.fn["reduce"](m, a, eps)
+
+    # structure-level arithmetic --------------------------------------------
+    def cpy(self, m: int, a, b) -> None:
+        self.fn["cpy"](m, a, b)
+
+    def scal(self, m: int, alpha: float, a) -> None:
+        self.fn["scal"](m, ctypes.byref(c_double(alpha)), a)
+
+    def axpy(self, m: int, alpha: float, a, b) -> None:
+        self.fn["axpy"](m, ctypes.byref(c_double(alpha)), a, b)
+
+    def adpy(self, m: int, alpha: float, d: np.ndarray, b) -> None:
+        self.fn["adpy"](m, ctypes.byref(c_double(alpha)), _ptr(d), b)

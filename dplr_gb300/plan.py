@@ -104,6 +104,20 @@ class GpuPlan:
         self.mixed = True
         self.mixed_slices = int(slices)
 
+    def scal(self, alpha: float, stream=None) -> None:
+        """A := alpha A on the device (dplrscal's sign convention); the
+        factorisation and sliced copies must be rebuilt afterwards."""
+        _native.check(_native.lib().dplr_gpu_scal(self._h, float(alpha), _stream_ptr(stream)), "dplr_gpu_scal")
+        self.factored = self.factored_transposed = self.sliced = self.mixed = False
+
+    def adpy(self, alpha: float, d: torch.Tensor, stream=None) -> None:
+        """A := alpha diag(d) + A on the device (d: CUDA float64, m entries)."""
+        if not (d.is_cuda and d.dtype == torch.float64 and d.is_contiguous() and d.numel() == self.m):
+            raise ValueError(f"d must be a contiguous CUDA float64 tensor of {self.m} entries")
+        _native.check(_native.lib().dplr_gpu_adpy(self._h, float(alpha), d.data_ptr(), _stream_ptr(stream)),
+                      "dplr_gpu_adpy")
+        self.factored = self.factored_transposed = self.sliced = self.mixed = False
+
     def prepare_pairs(self, stream=None) -> None:
         """Float-pair copy of the factors: 1-RHS op-N applies then run on the
         FP32 pipes (FP64-accurate, compensated sums) at HBM speed."""

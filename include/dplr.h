@@ -118,6 +118,24 @@ DPLR_API long int dplrnz(int m, DPlrMtx *A);
  * src/dplrp2d.c:98. */
 DPLR_API void dplrgep2d(int m, DPlrMtx *A, double *B, int ldb);
 
+/* B := A; B is rebuilt (dplrclr + dplrinid / dplrinih) where its type or
+ * size differs, and low-rank capacities grow to A's ranks.  Replaces
+ * dplrcpy, src/dplrcpy.c:19. */
+DPLR_API void dplrcpy(int m, DPlrMtx *A, DPlrMtx *B);
+
+/* A := alpha*A; low-rank blocks scale sig by |alpha| and negate u for
+ * alpha < 0.  Replaces dplrscal, src/dplrscal.c:17. */
+DPLR_API void dplrscal(int m, double *alpha, DPlrMtx *A);
+
+/* B := alpha*A + B for PLR matrices of the same shape: leaves add, low-rank
+ * blocks append A's columns (sig |alpha|, u negated for alpha < 0; capacity
+ * grown as needed).  Replaces dplraxpy, src/dplraxpy.c:81. */
+DPLR_API void dplraxpy(int m, double *alpha, DPlrMtx *A, DPlrMtx *B);
+
+/* B := alpha*diag(D) + B (D: the m diagonal entries).  Replaces dplradpy,
+ * src/dplraxpy.c:141. */
+DPLR_API void dplradpy(int m, double *alpha, double *D, DPlrMtx *B);
+
 /* ---- GPU hot path --------------------------------------------------- */
 
 /* y := alpha*op(A)*x + beta*y.  Replaces dplrgepmv, src/dplrpmv.c:262. */

@@ -71,6 +71,14 @@ DPLR_API int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha,
  * is outside 2^+-50 (FP32 range). */
 DPLR_API int dplr_gpu_prepare_pairs(dplr_gpu_plan plan, void *stream);
 
+/* Device-resident structure arithmetic on a plan (no host round trip):
+ * A := alpha*A (dplrscal's convention: sig scaled by |alpha|, u negated for
+ * alpha < 0) and A := alpha*diag(D) + A with D on the device (m entries,
+ * dplradpy).  The factorisation and sliced copies are dropped (rebuild them
+ * as after dplr_gpu_pool_write); a float-pair copy is rebuilt. */
+DPLR_API int dplr_gpu_scal(dplr_gpu_plan plan, double alpha, void *stream);
+DPLR_API int dplr_gpu_adpy(dplr_gpu_plan plan, double alpha, const double *D, void *stream);
+
 /* Woodbury factorisation of the planned matrix (replaces forming inv(A)
  * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):
  * leaf inverses, per-level panels Z = D^-1 W and capacitance inverses
