@@ -42,7 +42,12 @@ constexpr int M = 128, N = 64;
 constexpr int RANGE = 16;              // stages per exact read-out (256 inner elements)
 constexpr int TB_A = M * KB;           // elements of a 128-row tile-block
 constexpr int TB_B = N * KB;           // elements of a 64-row tile-block
-constexpr int THREADS = 320;
+constexpr int EW = 16;                 // epilogue warps: 4 per TMEM lane quadrant
+constexpr int CPW = 4 * N / EW;        // TMEM columns per epilogue warp
+constexpr int C4N = CPW / 4;           // 4-column read-out groups per epilogue warp
+constexpr int THREADS = 64 + 32 * EW;  // producer warp, MMA warp, epilogue warps
+// registers per thread of one CTA per SM (warps are allocated in groups of 4)
+constexpr int kRegs = (65536 / (((THREADS / 32 + 3) / 4) * 4 * 32)) & ~7;
 constexpr int kSmem = 192 * 1024;
 constexpr int kSpin = 1 << 22;
 
@@ -290,7 +295,7 @@ __device__ __forceinline__ void setup(Ctl &ctl, int warp, int lane)
             tc::mbar_init(&ctl.empty[s], 1);
         }
         tc::mbar_init(&ctl.accf, 1);
-        tc::mbar_init(&ctl.acce, 8);
+        tc::mbar_init(&ctl.acce, EW);
         ctl.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -336,7 +341,7 @@ __device__ __forceinline__ int nkb_of(int K) { return (K + KB - 1) / KB; }
 // added to Bin in FP64 (accurate far beyond the inner solve's slices); otherwise
 // all terms and Bin meet in a 128-bit fixed-point sum rounded once.
 template <int NS, int D, bool LEAN>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __maxnreg__(kRegs)
     expand_kernel(const XTerm *__restrict__ terms, const int *__restrict__ tile_row0,
                   const int *__restrict__ tile_begin, int ntiles, int njt, const bf16 *__restrict__ apool,
                   long long astride, const int *__restrict__ aexp, const bf16 *__restrict__ ts, long long tstride,
@@ -416,16 +421,16 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---------------------------------------------------- epilogue
         const int lq = warp & 3, ch = (warp - 2) >> 2;
         const int row = lq * 32 + lane;
-        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * 32);
+        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * CPW);
         int ec = 0;
         if constexpr (LEAN) {
-            // the item's exponents and its 32 values of Bin do not depend on
+            // the item's exponents and its CPW values of Bin do not depend on
             // the products: they are loaded before waiting for the MMAs (and
             // the next item's exponents before this item's output pass)
             auto meta = [&](int it, int &re, int &cel, int &nkb) {
                 const int tile = it / njt, jt = it % njt;
                 const XTerm tt = terms[tile_begin[tile]];
-                const int myj = jt * N + ch * 32 + lane;
+                const int myj = jt * N + ch * CPW + lane;
                 nkb = nkb_of(tt.K);
                 re = aexp[tt.aexp + row] - 7 * D + kLeanDrop<D>;
                 cel = myj < nrhs ? (tt.src == 0 ? texp[(long long)tt.blk * nrhs + myj] : xexp[myj]) : 0;
@@ -434,16 +439,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (blockIdx.x < nitems) meta(blockIdx.x, re, cel, nkb);
             for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
                 const int tile = it / njt, jt = it % njt;
-                const int j0 = jt * N + ch * 32;
+                const int j0 = jt * N + ch * CPW;
                 const int gr = tile_row0[tile] + row;
-                double bv[32];
+                double bv[CPW];
                 if (addb) {
 #pragma unroll
-                    for (int c = 0; c < 32; ++c) bv[c] = j0 + c < nrhs ? Bin[gr + (long long)(j0 + c) * ldbin] : 0.0;
+                    for (int c = 0; c < CPW; ++c) bv[c] = j0 + c < nrhs ? Bin[gr + (long long)(j0 + c) * ldbin] : 0.0;
                 }
-                long long acc[32];
+                long long acc[CPW];
 #pragma unroll
-                for (int c = 0; c < 32; ++c) acc[c] = 0;
+                for (int c = 0; c < CPW; ++c) acc[c] = 0;
                 bool ok = true;
                 for (int kb0 = 0; kb0 < nkb; kb0 += RANGE) {
                     if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
@@ -452,7 +457,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     fence_after();
 #pragma unroll
-                    for (int c4 = 0; c4 < 8; ++c4) {
+                    for (int c4 = 0; c4 < C4N; ++c4) {
                         long long W[4];
                         read4_64<D>(trow, c4, W);
 #pragma unroll
@@ -467,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int rcur = re, ccur = cel;
                 if (it + (int)gridDim.x < nitems) meta(it + gridDim.x, re, cel, nkb);
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
+                for (int c = 0; c < CPW; ++c) {
                     const int j = j0 + c;
                     const int ce = __shfl_sync(0xffffffffu, ccur, c);
                     if (j < nrhs) {
@@ -480,7 +485,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
             const int tile = it / njt, jt = it % njt;
             const int q0 = tile_begin[tile], q1 = tile_begin[tile + 1];
-            const int j0 = jt * N + ch * 32;         // this warp's first column
+            const int j0 = jt * N + ch * CPW;        // this warp's first column
             const int myj = j0 + lane;               // column whose exponents this lane holds
             // alignment exponents: the tile's largest row exponent per row and
             // column exponent per column (precomputed, or from the terms)
@@ -498,9 +503,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 if (rmax < -99999) rmax = 0;
                 if (cmaxl < -99999) cmaxl = 0;
             }
-            __int128 acc[32];
+            __int128 acc[CPW];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] = 0;
+            for (int c = 0; c < CPW; ++c) acc[c] = 0;
             bool ok = true;
             // a term's shifts and depth, loaded one term ahead of its read-out
             auto shifts = [&](int q, int &rd, int &cd, int &kbs) {
@@ -521,7 +526,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     fence_after();
 #pragma unroll
-                    for (int c4 = 0; c4 < 8; ++c4) {
+                    for (int c4 = 0; c4 < C4N; ++c4) {
                         __int128 W[4];
                         read4<D>(trow, c4, W);
 #pragma unroll
@@ -543,7 +548,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             // outputs: fold in +-Bin exactly, round once
             const int gr = tile_row0[tile] + row;
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
+            for (int c = 0; c < CPW; ++c) {
                 const int j = j0 + c;
                 const int cm = __shfl_sync(0xffffffffu, cmaxl, c);
                 if (j < nrhs) {
@@ -582,7 +587,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // ------------------------------------------------------------- panel
 // Work unit it = item * njp + jp (pairs of 64-column X tiles adjacent).
 template <int NS, int D>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __maxnreg__(kRegs)
     panel_kernel(const PItem *__restrict__ items, int nitems, int njp, const bf16 *__restrict__ vpool,
                  long long vstride, const bf16 *__restrict__ xs, long long xstride, int xnjt, int nrhs,
                  __int128 *__restrict__ partials, int *err)
@@ -645,15 +650,15 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else {
         const int lq = warp & 3, ch = (warp - 2) >> 2;
-        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * 32);
+        const uint32_t trow = ctl.tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(ch * CPW);
         int ec = 0;
         for (int u = blockIdx.x; u < nunits && !ctl.abort; u += gridDim.x) {
             const PItem itm = items[u / njp];
             const int jp = u % njp;
             const int ncol = min(itm.nr, itm.rank - itm.kt);     // live ranks of the tile
-            __int128 acc[32];
+            __int128 acc[CPW];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] = 0;
+            for (int c = 0; c < CPW; ++c) acc[c] = 0;
             bool ok = true;
             for (int kb0 = 0; kb0 < itm.nkb; kb0 += RANGE) {
                 if (!wait_bar(ctl, &ctl.accf, (uint32_t)(ec & 1))) {
@@ -664,7 +669,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 // columns past the tile's padded rank hold stale values; they
                 // are read (the loads are warp-collective) but never written
 #pragma unroll
-                for (int c4 = 0; c4 < 8; ++c4) {
+                for (int c4 = 0; c4 < C4N; ++c4) {
                     __int128 W[4];
                     read4<D>(trow, c4, W);
 #pragma unroll
@@ -679,10 +684,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int j = jp * M + lq * 32 + lane;                 // right-hand side of this lane
             if (j < nrhs) {
                 __int128 *P = partials + itm.p * nrhs + (long long)itm.chunk * itm.rank * nrhs +
-                              (long long)j * itm.rank + itm.kt + ch * 32;
+                              (long long)j * itm.rank + itm.kt + ch * CPW;
 #pragma unroll
-                for (int c = 0; c < 32; ++c)
-                    if (ch * 32 + c < ncol) P[c] = acc[c];
+                for (int c = 0; c < CPW; ++c)
+                    if (ch * CPW + c < ncol) P[c] = acc[c];
             }
         }
     }
