@@ -19,6 +19,7 @@
 #include "tcpipe.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -154,6 +155,35 @@ __device__ __forceinline__ void i128_to_dd(__int128 w, double &hi, double &lo)
 {
     hi = (double)w;
     lo = (double)(w - (__int128)hi);
+}
+
+// w 2^E as double-double with integer arithmetic only: hi = w rounded to 53
+// bits (nearest, ties to even), lo = the exact remainder rounded to 53 bits;
+// both scaled by 2^E through the exponent field.  GB300's FP64 rate makes
+// this much cheaper than the library's 128-bit conversions and ldexp.
+__device__ __forceinline__ void i128_to_dd_scaled(__int128 w, int E, double &hi, double &lo)
+{
+    if (w == 0) {
+        hi = lo = 0.0;
+        return;
+    }
+    const bool neg = w < 0;
+    const unsigned __int128 a = neg ? (unsigned __int128)(-w) : (unsigned __int128)w;
+    const unsigned long long ah = (unsigned long long)(a >> 64), al = (unsigned long long)a;
+    const int msb = ah ? 127 - __clzll((long long)ah) : 63 - __clzll((long long)al);
+    if (msb <= 52) {
+        hi = tc::i128_to_double(w, E);
+        lo = 0.0;
+        return;
+    }
+    const int sh = msb - 52;
+    unsigned __int128 m = a >> sh;
+    const unsigned __int128 rem = a - (m << sh), half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (m & 1))) ++m;            // may reach 2^53: still exact below
+    const __int128 hint = (__int128)(m << sh);                  // |w| rounded, exactly
+    const __int128 r = (__int128)a - hint;                      // |r| <= 2^(sh-1)
+    hi = tc::i128_to_double(neg ? -hint : hint, E);
+    lo = tc::i128_to_double(neg ? -r : r, E);
 }
 
 // One warp: 32 x 16 output block (2 x 2 fragments) for one slice pair over
@@ -437,33 +467,64 @@ __global__ void __launch_bounds__(kSThreads) sp_panel_kernel(
 }
 
 // Reduce: T = sig o 2^(E) sum_c W_c as double-double.
+// T = sig o (sum over chunks of the 128-bit partials), as double-double.
+// One thread per element of the schedule's concatenated element space:
+// item i owns [rsum_i nrhs, (rsum_i + rank_i) nrhs), its element e = k + j
+// rank; the item is found by binary search on rsum (no idle CTAs whatever
+// the ranks), and the chunk sums run four loads deep (integer sums, so the
+// order does not change the result).
 template <int DMAX>
-__global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items,
+__global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items, int nitems, long long total,
                                  const __int128 *__restrict__ partials, const int *__restrict__ aexp,
                                  const int *__restrict__ xexp, const double *__restrict__ sigbase,
                                  int nrhs, double *__restrict__ T, long long lo_off)
 {
-    const SReduceItem R = items[blockIdx.x];
-    const long long cnt = (long long)R.rank * nrhs;
-    const long long e = (long long)blockIdx.y * blockDim.x + threadIdx.x;
-    if (e >= cnt) return;
-    const int k = (int)(e % R.rank), j = (int)(e / R.rank);
-    __int128 W = 0;
-    for (int c = 0; c < R.nch; ++c) W += partials[R.p * nrhs + (long long)c * cnt + e];
-    double hi, lo;
-    i128_to_dd(W, hi, lo);
-    const int E = aexp[R.fexp + k] + xexp[j] - 7 * DMAX;
-    hi = ldexp(hi, E);
-    lo = ldexp(lo, E);
-    if (R.sig >= 0) {
-        const double s = sigbase[R.sig + k];
-        const double p = hi * s;
-        const double err = fma(hi, s, -p);
-        const double l2 = fma(lo, s, err);
-        two_sum(p, l2, hi, lo);
+    const long long E = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (E >= total) return;
+    const long long q = E / nrhs;
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].rsum <= q) lo = mid; else hi = mid - 1;
     }
-    T[R.t * nrhs + e] = hi;
-    T[lo_off + R.t * nrhs + e] = lo;
+    const SReduceItem R = items[lo];
+    const long long cnt = (long long)R.rank * nrhs;
+    const long long e = E - (long long)R.rsum * nrhs;
+    const int k = (int)(e % R.rank), j = (int)(e / R.rank);
+    const __int128 *P = partials + R.p * nrhs + e;
+    __int128 W0 = 0, W1 = 0, W2 = 0, W3 = 0;
+    int c = 0;
+    for (; c + 3 < R.nch; c += 4) {
+        W0 += P[(long long)c * cnt];
+        W1 += P[(long long)(c + 1) * cnt];
+        W2 += P[(long long)(c + 2) * cnt];
+        W3 += P[(long long)(c + 3) * cnt];
+    }
+    for (; c < R.nch; ++c) W0 += P[(long long)c * cnt];
+    const __int128 W = (W0 + W1) + (W2 + W3);
+    double hi2, lo2;
+    i128_to_dd_scaled(W, aexp[R.fexp + k] + xexp[j] - 7 * DMAX, hi2, lo2);
+    if (R.sig >= 0) {
+        // (hi2 + lo2) s as double-double: exact product of hi2, |l2| << |pr|
+        const double s = sigbase[R.sig + k];
+        const double pr = hi2 * s;
+        const double l2 = fma(lo2, s, fma(hi2, s, -pr));
+        hi2 = pr + l2;
+        lo2 = l2 - (hi2 - pr);
+    }
+    T[R.t * nrhs + e] = hi2;
+    T[lo_off + R.t * nrhs + e] = lo2;
+}
+
+template <int DMAX>
+static void launch_reduce(const SSchedule &S, const __int128 *partials, const int *aexp, const int *xexp,
+                          const double *sigbase, int nrhs, double *T, long long lo_off, cudaStream_t st)
+{
+    const long long total = (long long)S.rtotal * nrhs;
+    if (S.reduces.empty() || total == 0) return;
+    sp_reduce_kernel<DMAX><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
+        S.d_reduces, (int)S.reduces.size(), total, partials, aexp, xexp, sigbase, nrhs, T, lo_off);
+    note_launch();
 }
 
 // Slices of the double-double panel results, one exponent per (block,
@@ -732,6 +793,11 @@ static size_t panel_smem(int nsa, int nsb) { return (size_t)(nsa + nsb) * ST * S
 static int upload_sschedule(SSchedule &A, long long *bytes)
 {
     int rc;
+    A.rtotal = 0;
+    for (SReduceItem &r : A.reduces) {
+        r.rsum = A.rtotal;
+        A.rtotal += r.rank;
+    }
     if ((rc = dev_vec(A.items, &A.d_items, bytes)) || (rc = dev_vec(A.reduces, &A.d_reduces, bytes)) ||
         (rc = dev_vec(A.tile_row0, &A.d_tile_row0, bytes)) ||
         (rc = dev_vec(A.tile_begin, &A.d_tile_begin, bytes)) || (rc = dev_vec(A.terms, &A.d_terms, bytes)))
@@ -993,10 +1059,7 @@ int sliced_residual(Plan *p, int nrhs, const double *X, int ldx, const double *B
             DG_CUDA(cudaGetLastError());
         }
         ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
-        long long maxcnt = (long long)A.max_rank * nrhs;
-        sp_reduce_kernel<kD><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
-            A.d_reduces, w.partials, S->exps, S->xexp, p->pool, nrhs, w.T, w.lo_off);
-        note_launch();
+        launch_reduce<kD>(A, w.partials, S->exps, S->xexp, p->pool, nrhs, w.T, w.lo_off, st);
         long long warps = (long long)A.reduces.size() * nrhs;
         sp_tslice_kernel<kNS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
             A.d_reduces, (int)A.reduces.size(), w.T, w.lo_off, nrhs, w.ts, w.tstride, w.texp);
@@ -1369,10 +1432,7 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
             ProfScope ps("mixed_panel", st, fl * npairs, 0.0);
             launch_panel<NS, D>(p, S, M->pool, M->stride, M->xs, xstride, m, nrhs, w.partials, st);
         }
-        long long maxcnt = (long long)S.max_rank * nrhs;
-        sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
-            S.d_reduces, w.partials, M->exps, M->xexp, p->pool, nrhs, w.T, w.lo_off);
-        note_launch();
+        launch_reduce<D>(S, w.partials, M->exps, M->xexp, p->pool, nrhs, w.T, w.lo_off, st);
         DG_CUDA(cudaGetLastError());
         // capacitance in FP64 on the high parts
         if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, w.T, w.W, nrhs, st))) return rc;
@@ -1579,37 +1639,59 @@ __global__ void xslice_tb_kernel(const double *__restrict__ X, int m, int ldx, i
 // 64 columns x 16 ranks, one exponent per (block, column); one warp per
 // (block, column j < njt * 64).
 template <int NS>
-__global__ void tslice_tb_kernel(const SReduceItem *__restrict__ items, int nitems, const double *__restrict__ T,
-                                 long long lo_off, int nrhs, int njt, bf16 *__restrict__ ts, long long tstride,
-                                 int *__restrict__ texp)
+__global__ void __launch_bounds__(256) tslice_tb_kernel(const SReduceItem *__restrict__ items, int nitems,
+                                                        const double *__restrict__ T, long long lo_off, int nrhs,
+                                                        int njt, bf16 *__restrict__ ts, long long tstride,
+                                                        int *__restrict__ texp)
 {
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int ncol = njt * 64;
-    if (w >= (long long)nitems * ncol) return;
-    const int b = (int)(w / ncol), j = (int)(w % ncol);
+    // one CTA per (block, 64-column tile); thread = (column jl, 8 ranks kg)
+    __shared__ int cexp[64];
+    const int b = blockIdx.x, jt = blockIdx.y;
+    if (b >= nitems) return;
     const SReduceItem R = items[b];
-    const bool live = j < nrhs;
-    const double *th = T + R.t * nrhs + (long long)(live ? j : 0) * R.rank;
-    const double *tl = lo_off >= 0 ? th + lo_off : nullptr;
-    double mx = 0.0;
-    if (live)
-        for (int k = lane; k < R.rank; k += 32) mx = fmax(mx, fabs(th[k]));
+    const int ngrp = R.rp >> 3;                   // 8-rank groups of the padded rank
+    if (threadIdx.x < 64) cexp[threadIdx.x] = INT_MIN;
+    __syncthreads();
+    // column exponents: scale_exp is monotone, so the max of the per-thread
+    // exponents is the exponent of the column's largest entry
+    for (int w = threadIdx.x; w < 64 * ngrp; w += blockDim.x) {
+        const int jl = w & 63, kg = w >> 6, j = jt * 64 + jl;
+        if (j >= nrhs) continue;
+        const double *th = T + R.t * nrhs + (long long)j * R.rank;
+        double mx = 0.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    const int e = scale_exp(mx);
-    if (live && lane == 0) texp[(long long)b * nrhs + j] = e;
-    const int nkb = R.rp >> 4;
-    bf16 *base = ts + R.tpad * njt + (long long)(j >> 6) * nkb * kTbB;
-    for (int k = lane; k < nkb * 16; k += 32) {
-        bf16 *o = base + (long long)(k >> 4) * kTbB + tc2::tbo(j & 63, k & 15);
-        if (live && k < R.rank) {
-            slice_dd<NS>(th[k], tl ? tl[k] : 0.0, e, o, tstride);
-        } else {
-            const bf16 zero = __float2bfloat16(0.0f);
-#pragma unroll
-            for (int p = 0; p < NS; ++p) o[p * tstride] = zero;
+        for (int u = 0; u < 8; ++u) {
+            const int k = kg * 8 + u;
+            if (k < R.rank) mx = fmax(mx, fabs(th[k]));
         }
+        if (mx > 0.0) atomicMax(&cexp[jl], scale_exp(mx));
+    }
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        if (cexp[threadIdx.x] == INT_MIN) cexp[threadIdx.x] = 0;     // all-zero column
+        if (jt * 64 + threadIdx.x < nrhs) texp[(long long)b * nrhs + jt * 64 + threadIdx.x] = cexp[threadIdx.x];
+    }
+    __syncthreads();
+    bf16 *base = ts + R.tpad * njt + (long long)jt * (R.rp >> 4) * kTbB;
+    for (int w = threadIdx.x; w < 64 * ngrp; w += blockDim.x) {
+        const int jl = w & 63, kg = w >> 6, j = jt * 64 + jl;
+        const int k0 = kg * 8;
+        bf16 *o = base + (long long)(k0 >> 4) * kTbB + tc2::tbo(jl, k0 & 15);
+        long long y[8];
+        if (j < nrhs) {
+            const double *th = T + R.t * nrhs + (long long)j * R.rank;
+            const double *tl = lo_off >= 0 ? th + lo_off : nullptr;
+            const int sh = 7 * NS - cexp[jl];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = k0 + u;
+                y[u] = k < R.rank ? scaled_int(th[k], sh) + (tl ? scaled_int(tl[k], sh) : 0) : 0;
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) y[u] = 0;
+        }
+        store8<NS>(y, o, tstride);
     }
 }
 
@@ -1644,6 +1726,11 @@ __global__ void tile_cmax_kernel(const XTerm *__restrict__ terms, const int *__r
 int upload_tb(SSchedule &S, long long *bytes)
 {
     int rc;
+    S.rtotal = 0;
+    for (SReduceItem &r : S.reduces) {
+        r.rsum = S.rtotal;
+        S.rtotal += r.rank;
+    }
     if ((rc = dev_vec(S.pitems, &S.d_pitems, bytes)) || (rc = dev_vec(S.reduces, &S.d_reduces, bytes)) ||
         (rc = dev_vec(S.tile_row0, &S.d_tile_row0, bytes)) || (rc = dev_vec(S.tile_begin, &S.d_tile_begin, bytes)) ||
         (rc = dev_vec(S.xterms, &S.d_xterms, bytes)))
@@ -2001,13 +2088,12 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
             launch_panel_tb<NSR, DR>(p, A, S->pool, S->stride, S->xs, m, nrhs, partials, st);
             DG_CUDA(cudaGetLastError());
         }
-        ProfScope ps2("sliced_reduce", st, 0.0, 0.0);
-        const long long maxcnt = (long long)A.max_rank * nrhs;
-        sp_reduce_kernel<DR><<<dim3((unsigned)A.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
-            A.d_reduces, partials, S->exps, S->xexp, p->pool, nrhs, T, lo_off);
-        note_launch();
-        const long long warps = (long long)A.reduces.size() * njt * 64;
-        tslice_tb_kernel<NSR><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+        {
+            ProfScope ps2("sliced_reduce", st, 0.0, 16.0 * A.partial_per_rhs * nrhs);
+            launch_reduce<DR>(A, partials, S->exps, S->xexp, p->pool, nrhs, T, lo_off, st);
+        }
+        ProfScope ps3("sliced_tslice", st, 0.0, 0.0);
+        tslice_tb_kernel<NSR><<<dim3((unsigned)A.reduces.size(), (unsigned)njt), 256, 0, st>>>(
             A.d_reduces, (int)A.reduces.size(), T, lo_off, nrhs, njt, ts, tstride, texp);
         note_launch();
         DG_CUDA(cudaGetLastError());
@@ -2235,19 +2321,15 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
             ProfScope ps("mixed_panel", st, fl * npairs, 0.0);
             launch_panel_tb<NS, D>(p, S, M->pool, M->stride, M->xs, m, nrhs, partials, st);
         }
-        const long long maxcnt = (long long)S.max_rank * nrhs;
         {
             ProfScope ps("mixed_reduce", st, 0.0, 0.0);
-            sp_reduce_kernel<D><<<dim3((unsigned)S.reduces.size(), (unsigned)((maxcnt + 255) / 256)), 256, 0, st>>>(
-                S.d_reduces, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off);
-            note_launch();
+            launch_reduce<D>(S, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off, st);
             DG_CUDA(cudaGetLastError());
         }
         if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
         {
-            ProfScope ps("mixed_reduce", st, 0.0, 0.0);
-            const long long warps = (long long)S.reduces.size() * njt * 64;
-            tslice_tb_kernel<NS><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            ProfScope ps("mixed_tslice", st, 0.0, 0.0);
+            tslice_tb_kernel<NS><<<dim3((unsigned)S.reduces.size(), (unsigned)njt), 256, 0, st>>>(
                 S.d_reduces, (int)S.reduces.size(), W, -1, nrhs, njt, ws, wstride, wexp);
             note_launch();
         }

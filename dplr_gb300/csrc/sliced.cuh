@@ -41,6 +41,7 @@ struct SReduceItem {
     int rank, nch, fexp;
     int rp;             // padded rank
     long long tpad;     // offset / nrhs of the block's T-slice panel
+    int rsum;           // ranks of the schedule's earlier items (the reduce's element space)
 };
 
 // Term of a sliced output tile: acc += A[tile rows, 0:K] * B[0:K, :], A
@@ -92,6 +93,7 @@ struct SSchedule {
     long long t_per_rhs = 0;        // DD T entries / nrhs
     long long tpad_per_rhs = 0;     // T-slice entries / nrhs
     int max_rank = 0;
+    int rtotal = 0;                 // sum of the reduce items' ranks
     std::vector<int> tile_row0, tile_begin;
     std::vector<STerm> terms;
     SPanelItem *d_items = nullptr;
