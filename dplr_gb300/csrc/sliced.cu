@@ -1502,6 +1502,7 @@ int pad16(int x) { return (x + 15) & ~15; }
 // V into tile-blocks: one CTA per (job, rank column).
 struct VSliceJob {
     long long src;          // column-major n x rank (ld n)
+    long long sig;          // pool offset of sig (columns sliced as V sig_k), or -1
     long long dst[4];       // tile-block base of rank tiles 0..3
     int nr[4];              // padded rows of those tiles
     int n, rank, exp;
@@ -1521,8 +1522,11 @@ __global__ void slice_v_tb_kernel(const VSliceJob *jobs, const int *col_base, in
     const VSliceJob &J = jobs[lo];
     const int k = gc - col_base[lo];
     const double *col = src + J.src + (long long)k * J.n;
+    // with sig folded in, the column is the exact product V sig_k (TwoProd:
+    // p + err); a rounded |p| below 2^e keeps the exact value below 2^e
+    const double s = J.sig >= 0 ? src[J.sig + k] : 1.0;
     double mx = 0.0;
-    for (int i = threadIdx.x; i < J.n; i += blockDim.x) mx = fmax(mx, fabs(col[i]));
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) mx = fmax(mx, fabs(col[i] * s));
     red[threadIdx.x] = mx;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -1533,8 +1537,15 @@ __global__ void slice_v_tb_kernel(const VSliceJob *jobs, const int *col_base, in
     if (threadIdx.x == 0) exps[J.exp + k] = e;
     const int kt = k / 64, r = k % 64, nr = J.nr[kt];
     bf16 *base = dst + J.dst[kt];
-    for (int i = threadIdx.x; i < J.n; i += blockDim.x)
-        slice_d<NS>(col[i], e, base + (long long)(i >> 4) * nr * 16 + tc2::tbo(r, i & 15), stride);
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) {
+        bf16 *o = base + (long long)(i >> 4) * nr * 16 + tc2::tbo(r, i & 15);
+        if (J.sig >= 0) {
+            const double pr = col[i] * s;
+            slice_dd<NS>(pr, fma(col[i], s, -pr), e, o, stride);
+        } else {
+            slice_d<NS>(col[i], e, o, stride);
+        }
+    }
 }
 
 // Row-sliced operands into 128-row tile-blocks.
@@ -1745,8 +1756,10 @@ struct VLayout {
     int ncols = 0;
 };
 
+// fold_sig: slice V diag(sig) (the panel then yields T = S V^T x directly and
+// the reduce does no FP64 scaling).
 long long layout_v(const Plan *p, std::vector<std::array<long long, 4>> &vdst, std::vector<std::array<int, 4>> &vnr,
-                   long long el, const std::vector<int> &ev_off, VLayout &VL)
+                   long long el, const std::vector<int> &ev_off, VLayout &VL, bool fold_sig)
 {
     vdst.assign(p->lr.size(), {0, 0, 0, 0});
     vnr.assign(p->lr.size(), {0, 0, 0, 0});
@@ -1755,6 +1768,7 @@ long long layout_v(const Plan *p, std::vector<std::array<long long, 4>> &vdst, s
         if (L.rank == 0) continue;
         VSliceJob J{};
         J.src = L.v;
+        J.sig = fold_sig ? L.sig : -1;
         J.n = L.n;
         J.rank = L.rank;
         J.exp = ev_off[b];
@@ -1912,7 +1926,7 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     VLayout VL;
     std::vector<std::array<long long, 4>> vdst;
     std::vector<std::array<int, 4>> vnr;
-    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL);
+    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL, true);
     // every U row and leaf row has its own exponent
     std::vector<long long> ua(p->lr.size(), 0), la(p->leaves.size(), 0);
     std::vector<RSliceJob> uj, lj;
@@ -1990,7 +2004,7 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
         const int nch = (L.n + 1023) / 1024;
         const int nkb = (L.rank + 15) / 16;
         ridx[b] = (int)A.reduces.size();
-        A.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], nkb * 16, tpre});
+        A.reduces.push_back(SReduceItem{poff, L.toff, -1, L.rank, nch, ev_off[b], nkb * 16, tpre});   // sig in V
         poff += (long long)nch * L.rank;
         tpre += (long long)nkb * kTbB;
         A.max_rank = std::max(A.max_rank, L.rank);
@@ -2138,7 +2152,7 @@ static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
     VLayout VL;
     std::vector<std::array<long long, 4>> vdst;
     std::vector<std::array<int, 4>> vnr;
-    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL);
+    long long el = layout_v(p, vdst, vnr, 0, ev_off, VL, true);
     std::vector<long long> za(nlev, 0), la(p->leaves.size(), 0);
     std::vector<int> nkbw(nlev, 0);
     std::vector<RSliceJob> zj, lj;
@@ -2225,7 +2239,7 @@ static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
             panel_items(L, vdst[b], vnr[b], poff, S.pitems);
             const int nch = (L.n + 1023) / 1024;
             const int ridx = (int)S.reduces.size();
-            S.reduces.push_back(SReduceItem{poff, L.toff, L.sig, L.rank, nch, ev_off[b], pad16(L.rank), tpre[b]});
+            S.reduces.push_back(SReduceItem{poff, L.toff, -1, L.rank, nch, ev_off[b], pad16(L.rank), tpre[b]});   // sig in V
             poff += (long long)nch * L.rank;
             S.max_rank = std::max(S.max_rank, L.rank);
             for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += tc2::M) {
