@@ -1104,6 +1104,7 @@ void mixed_free(Plan *p)
     free_sschedule(M->leaf);
     cudaFree(M->xs);
     cudaFree(M->xexp);
+    cudaFree(M->xexp2);
     cudaFree(M->work);
     delete M;
     p->mixed = nullptr;
@@ -1815,8 +1816,10 @@ int xnjt_of(int nrhs) { return 2 * ((nrhs + 127) / 128); }
 
 // X slices (tile-blocks) and their exponents for nrhs columns.
 template <int NS>
+// known_exps: xexp already holds the column exponents (gathered by the
+// expand that wrote X, kNoExp for all-zero columns); only the fix-up runs.
 int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_elems, int *&xexp, size_t &xexp_n,
-               cudaStream_t st)
+               cudaStream_t st, bool known_exps = false)
 {
     const int xnjt = xnjt_of(nrhs);
     const size_t need = (size_t)NS * (m / 16) * xnjt * kTbB;
@@ -1835,7 +1838,12 @@ int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
         xexp_n = nrhs;
     }
-    xcol_exps(X, m, ldx, nrhs, xexp, st);
+    if (known_exps) {
+        xcol_fix_kernel<<<(nrhs + 255) / 256, 256, 0, st>>>(xexp, nrhs);
+        note_launch();
+    } else {
+        xcol_exps(X, m, ldx, nrhs, xexp, st);
+    }
     const long long cnt = (long long)(m / 16) * 2 * xnjt * 64;
     const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
     xslice_tb_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
@@ -1882,7 +1890,7 @@ template <int NS, int D>
 void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
                       const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, int m, const int *xexp,
                       int nrhs, bool neg, const double *Bin, int ldbin, bool addb, double *Y, int ldy,
-                      cudaStream_t st, const int *rmaxt = nullptr, const int *cmaxt = nullptr)
+                      cudaStream_t st, const int *rmaxt = nullptr, const int *cmaxt = nullptr, int *yexp = nullptr)
 {
     const int njt = (nrhs + 63) / 64;
     const int nt = (int)S.tile_row0.size();
@@ -1895,14 +1903,14 @@ void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long
             tc2::expand_kernel<NS, D, true><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
                 S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs,
                 xstride, xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, nullptr, nullptr,
-                p->tc_err_d);
+                nrhs <= tc2::kColCap ? yexp : nullptr, p->tc_err_d);
             note_launch();
             return;
         }
     }
     tc2::expand_kernel<NS, D, false><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
         S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs, xstride,
-        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, rmaxt, cmaxt, p->tc_err_d);
+        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, rmaxt, cmaxt, nullptr, p->tc_err_d);
     note_launch();
 }
 
@@ -2308,10 +2316,34 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
     const double npairs = pair_count(NS, D);
     int rc;
 
+    // The expand that writes X gathers X's column exponents (into xexp2,
+    // while xexp still describes the slices being read), so slicing X for the
+    // next level needs no exponent pass over it.
+    const bool gather = nrhs <= tc2::kColCap;
+    if (gather && M->xexp2_n < (size_t)nrhs) {
+        cudaFree(M->xexp2);
+        M->xexp2 = nullptr;
+        M->xexp2_n = 0;
+        if (cudaMalloc((void **)&M->xexp2, nrhs * sizeof(int)) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate exponents");
+        M->xexp2_n = nrhs;
+    }
+    auto start_gather = [&]() {
+        if (!gather) return;
+        xcol_init_kernel<<<(nrhs + 255) / 256, 256, 0, st>>>(M->xexp2, nrhs);
+        note_launch();
+    };
+    auto end_gather = [&]() {
+        if (!gather) return;
+        std::swap(M->xexp, M->xexp2);
+        std::swap(M->xexp_n, M->xexp2_n);
+    };
+
     // leaf step: X = Leaf^-1 B
     {
         ProfScope ps("mixed_slice_x", st, 0.0, (8.0 + 2.0 * NS) * m * nrhs);
         if ((rc = slice_x_tb<NS>(B, m, ldb, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+        start_gather();
     }
     {
         const SSchedule &LS = M->leaf;
@@ -2319,15 +2351,17 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
         for (const XTerm &t : LS.xterms) fl += 2.0 * tc2::M * t.K * nrhs;
         ProfScope ps("mixed_expand", st, fl * npairs, 0.0);
         launch_expand_tb<NS, D>(p, LS, M->pool, M->stride, M->exps, ws, wstride, wexp, M->xs, m, M->xexp, nrhs, false,
-                                nullptr, 0, false, X, ldx, st);
+                                nullptr, 0, false, X, ldx, st, nullptr, nullptr, gather ? M->xexp2 : nullptr);
         DG_CUDA(cudaGetLastError());
+        end_gather();
     }
     for (int l = (int)M->level.size() - 1; l >= 0; --l) {
         const SSchedule &S = M->level[l];
         if (S.pitems.empty()) continue;
         {
             ProfScope ps("mixed_slice_x", st, 0.0, (8.0 + 2.0 * NS) * m * nrhs);
-            if ((rc = slice_x_tb<NS>(X, m, ldx, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st))) return rc;
+            if ((rc = slice_x_tb<NS>(X, m, ldx, nrhs, M->xs, M->xs_elems, M->xexp, M->xexp_n, st, gather)))
+                return rc;
         }
         double fl = 0;
         for (const PItem &it : S.pitems) fl += 2.0 * it.nkb * 16 * std::min(64, it.rank - it.kt) * nrhs;
@@ -2346,13 +2380,15 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
             tslice_tb_kernel<NS><<<dim3((unsigned)S.reduces.size(), (unsigned)njt), 256, 0, st>>>(
                 S.d_reduces, (int)S.reduces.size(), W, -1, nrhs, njt, ws, wstride, wexp);
             note_launch();
+            start_gather();
         }
         double fu = 0;
         for (const XTerm &t : S.xterms) fu += 2.0 * tc2::M * t.K * nrhs;
         ProfScope ps2("mixed_expand", st, fu * npairs, 0.0);
         launch_expand_tb<NS, D>(p, S, M->pool, M->stride, M->exps, ws, wstride, wexp, M->xs, m, M->xexp, nrhs, true, X,
-                                ldx, true, X, ldx, st);
+                                ldx, true, X, ldx, st, nullptr, nullptr, gather ? M->xexp2 : nullptr);
         DG_CUDA(cudaGetLastError());
+        end_gather();
     }
     return 0;
 }

@@ -138,6 +138,8 @@ struct MixedSliced {
     size_t xs_elems = 0;
     int *xexp = nullptr;
     size_t xexp_n = 0;
+    int *xexp2 = nullptr;          // exponents of the X being written (swapped with xexp)
+    size_t xexp2_n = 0;
     void *work = nullptr;
     size_t work_bytes = 0;
     long long bytes = 0;

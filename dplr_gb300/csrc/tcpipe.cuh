@@ -49,6 +49,8 @@ constexpr int THREADS = 64 + 32 * EW;  // producer warp, MMA warp, epilogue warp
 // registers per thread of one CTA per SM (warps are allocated in groups of 4)
 constexpr int kRegs = (65536 / (((THREADS / 32 + 3) / 4) * 4 * 32)) & ~7;
 constexpr int kSmem = 192 * 1024;
+constexpr int kColCap = 1024;          // right-hand sides whose output exponents the lean expand gathers
+constexpr int kNoExpT = -(1 << 24);    // "no entry" exponent (below every finite one)
 constexpr int kSpin = 1 << 22;
 
 template <int NS>
@@ -348,12 +350,18 @@ __global__ void __maxnreg__(kRegs)
                   const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int xnjt,
                   const int *__restrict__ xexp, int nrhs, int neg, const double *__restrict__ Bin, int ldbin,
                   int addb, double *__restrict__ Y, int ldy, const int *__restrict__ rmaxt,
-                  const int *__restrict__ cmaxt, int *err)
+                  const int *__restrict__ cmaxt, int *__restrict__ yexp, int *err)
 {
     using C = Cfg<NS>;
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ Ctl ctl;
+    // lean expand with yexp: per right-hand side the largest exponent of the
+    // outputs written (the next slicing of Y needs it); gathered per CTA here
+    __shared__ int colmax[LEAN ? kColCap : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if constexpr (LEAN)
+        if (yexp)
+            for (int j = threadIdx.x; j < min(nrhs, kColCap); j += blockDim.x) colmax[j] = kNoExpT;
     setup<NS, D>(ctl, warp, lane);
     const uint32_t sbase = su32(smem);
     const int nitems = ntiles * njt;
@@ -475,11 +483,29 @@ __global__ void __maxnreg__(kRegs)
                 for (int c = 0; c < CPW; ++c) {
                     const int j = j0 + c;
                     const int ce = __shfl_sync(0xffffffffu, ccur, c);
+                    double y = 0.0;
                     if (j < nrhs) {
                         const double t = i64_scaled(neg ? -acc[c] : acc[c], rcur + ce);
-                        Y[gr + (long long)j * ldy] = addb ? bv[c] + t : t;
+                        y = addb ? bv[c] + t : t;
+                        Y[gr + (long long)j * ldy] = y;
+                    }
+                    if (yexp) {
+                        // exponent e with |y| < 2^e from the bits (subnormals: ilogb)
+                        const int be = (int)((__double_as_longlong(y) >> 52) & 0x7FF);
+                        int e = kNoExpT;
+                        if (be > 0 && be < 0x7FF) e = be - 1022;
+                        else if (be == 0 && y != 0.0) e = ilogb(fabs(y)) + 1;
+                        e = __reduce_max_sync(0xffffffffu, e);
+                        if (lane == c && j < min(nrhs, kColCap) && e > kNoExpT) atomicMax(&colmax[j], e);
                     }
                 }
+            }
+            if (yexp) {
+                // every epilogue warp leaves the item loop exactly once: named
+                // barrier over the epilogue threads, then one flush per CTA
+                asm volatile("bar.sync 1, %0;" ::"r"(EW * 32) : "memory");
+                for (int j = threadIdx.x - 64; j < min(nrhs, kColCap); j += EW * 32)
+                    if (colmax[j] > kNoExpT) atomicMax(&yexp[j], colmax[j]);
             }
         } else
         for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
