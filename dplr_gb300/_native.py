@@ -48,6 +48,7 @@ def _bind(lib: ctypes.CDLL) -> None:
                                           POINTER(c_int), c_void_p])
     sig("dplr_gpu_prepare_sliced", c_int, [c_void_p, c_void_p])
     sig("dplr_gpu_prepare_mixed", c_int, [c_void_p, c_int, c_void_p])
+    sig("dplr_gpu_prepare_mixed_caps", c_int, [c_void_p, c_int, c_int, c_void_p])
     sig("dplr_gpu_prepare_pairs", c_int, [c_void_p, c_void_p])
     sig("dplr_gpu_scal", c_int, [c_void_p, c_double, c_void_p])
     sig("dplr_gpu_adpy", c_int, [c_void_p, c_double, c_void_p, c_void_p])

@@ -525,19 +525,19 @@ int run_expand(const Schedule &S, const double *abase, const double *T, const do
     return 0;
 }
 
-int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int trans,
-             const double *T, double *W, int nrhs, cudaStream_t st)
+int run_cap_list(const std::vector<CapItem> &caps, const CapItem *d_caps, const double *kbase, const double *sigbase,
+                 int trans, const double *T, double *W, int nrhs, cudaStream_t st)
 {
-    if (S.caps.empty() || nrhs <= 0) return 0;
-    for (const CapItem &c : S.caps)
+    if (caps.empty() || nrhs <= 0) return 0;
+    for (const CapItem &c : caps)
         if (c.r1 + c.r2 > 4 * kThreads)
             return fail(DPLR_GPU_EINVAL, "capacitance of order %d exceeds %d", c.r1 + c.r2,
                         4 * kThreads);
     const int nb = std::min(pick_nb(nrhs), 8);
-    dim3 g((unsigned)S.caps.size(), (unsigned)((nrhs + nb - 1) / nb));
+    dim3 g((unsigned)caps.size(), (unsigned)((nrhs + nb - 1) / nb));
     const int scaled = sigbase != nullptr;
     double fl = 0, by = 0;
-    for (const CapItem &c : S.caps) {
+    for (const CapItem &c : caps) {
         double r = c.r1 + c.r2;
         fl += 2.0 * r * r * nrhs;
         by += 8.0 * (r * r + 2.0 * r * nrhs);
@@ -545,13 +545,19 @@ int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int 
     ProfScope ps("capacitance", st, fl, by);
     note_launch();
     switch (nb) {
-    case 8: cap_kernel<8><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
-    case 4: cap_kernel<4><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
-    case 2: cap_kernel<2><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
-    default: cap_kernel<1><<<g, kThreads, 0, st>>>(S.d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    case 8: cap_kernel<8><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    case 4: cap_kernel<4><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    case 2: cap_kernel<2><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
+    default: cap_kernel<1><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
     }
     DG_CUDA(cudaGetLastError());
     return 0;
+}
+
+int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int trans, const double *T, double *W,
+             int nrhs, cudaStream_t st)
+{
+    return run_cap_list(S.caps, S.d_caps, kbase, sigbase, trans, T, W, nrhs, st);
 }
 
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,

@@ -190,6 +190,8 @@ int run_expand(const Schedule &S, const double *abase, const double *T, const do
                double *Y, int ldy, int nrhs, double alpha, double beta, cudaStream_t st);
 int run_caps(const Schedule &S, const double *kbase, const double *sigbase, int trans,
              const double *T, double *W, int nrhs, cudaStream_t st);
+int run_cap_list(const std::vector<CapItem> &caps, const CapItem *d_caps, const double *kbase, const double *sigbase,
+                 int trans, const double *T, double *W, int nrhs, cudaStream_t st);
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,
                  double beta, double *Y, int ldy, cudaStream_t st, bool alpha0_squares_beta);
 int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream_t st);

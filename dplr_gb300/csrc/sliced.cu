@@ -19,6 +19,7 @@
 #include "tcpipe.cuh"
 
 #include <algorithm>
+#include <unordered_map>
 #include <climits>
 #include <array>
 #include <cmath>
@@ -1106,6 +1107,10 @@ void mixed_free(Plan *p)
     cudaFree(M->xexp);
     cudaFree(M->xexp2);
     cudaFree(M->work);
+    cudaFree(M->kslices);
+    cudaFree(M->kexps);
+    for (SSchedule &C : M->capsched) free_sschedule(C);
+    for (CapItem *d : M->d_capfb) cudaFree(d);
     delete M;
     p->mixed = nullptr;
 }
@@ -1169,7 +1174,7 @@ out:
     return rc;
 }
 
-int mixed_build(Plan *p, int ns, cudaStream_t st)
+int mixed_build(Plan *p, int ns, cudaStream_t st, bool fp64_caps)
 {
     mixed_free(p);
     Fact *F = (Fact *)p->fact;
@@ -1182,6 +1187,7 @@ int mixed_build(Plan *p, int ns, cudaStream_t st)
     MixedSliced *M = new MixedSliced();
     p->mixed = M;
     M->ns = ns;
+    M->tc_caps = !fp64_caps;
     if (sliced_tile_rows(p) == tc::M) {
         switch (ns) {
         case 3: return mixed_build_tb_t<3>(p, M, F, st);
@@ -1890,7 +1896,8 @@ template <int NS, int D>
 void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long long astride, const int *aexp,
                       const bf16 *ts, long long tstride, const int *texp, const bf16 *xs, int m, const int *xexp,
                       int nrhs, bool neg, const double *Bin, int ldbin, bool addb, double *Y, int ldy,
-                      cudaStream_t st, const int *rmaxt = nullptr, const int *cmaxt = nullptr, int *yexp = nullptr)
+                      cudaStream_t st, const int *rmaxt = nullptr, const int *cmaxt = nullptr, int *yexp = nullptr,
+                      int rscale = 1)
 {
     const int njt = (nrhs + 63) / 64;
     const int nt = (int)S.tile_row0.size();
@@ -1903,14 +1910,15 @@ void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long
             tc2::expand_kernel<NS, D, true><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
                 S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs,
                 xstride, xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, nullptr, nullptr,
-                nrhs <= tc2::kColCap ? yexp : nullptr, p->tc_err_d);
+                nrhs <= tc2::kColCap ? yexp : nullptr, rscale, p->tc_err_d);
             note_launch();
             return;
         }
     }
     tc2::expand_kernel<NS, D, false><<<grid_of((long long)nt * njt), tc2::THREADS, tc2::Cfg<NS>::SMEM, st>>>(
         S.d_xterms, S.d_tile_row0, S.d_tile_begin, nt, njt, apool, astride, aexp, ts, tstride, texp, xs, xstride,
-        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, rmaxt, cmaxt, nullptr, p->tc_err_d);
+        xnjt_of(nrhs), xexp, nrhs, neg ? 1 : 0, Bin, ldbin, addb ? 1 : 0, Y, ldy, rmaxt, cmaxt, nullptr, rscale,
+        p->tc_err_d);
     note_launch();
 }
 
@@ -2138,6 +2146,75 @@ static int sliced_residual_tb(Plan *p, Sliced *S, int nrhs, const double *X, int
 }
 
 // -------------------------------------------------- mixed inner solve
+// Tensor-core capacitance: per level, the nodes whose two blocks both have
+// rank 128 get K^-1 (256 x 256, FP64) cut into 8 exact slices with row
+// exponents; K^-1 [T1; T2] is then two output tiles of 128 rows (the W of
+// the ne and of the sw block, ld 128, at T offset * nrhs), each the sum of
+// two terms K^-1[tile, 0:128] T1 + K^-1[tile, 128:256] T2 with the T slices'
+// own column exponents -- the multi-term expand, products exact, one
+// rounding per output (at least FP64 accuracy).  Other nodes stay on the
+// FP64 kernel.
+static int build_tc_caps(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
+{
+    const int nlev = (int)F->lv.size();
+    M->capsched.assign(nlev, SSchedule());
+    M->capfb.assign(nlev, std::vector<CapItem>());
+    M->d_capfb.assign(nlev, nullptr);
+    std::vector<RSliceJob> kj;
+    std::vector<int> kb;
+    long long kel = 0;
+    int krows = 0, kexp = 0, rc;
+    for (int l = 0; l < nlev; ++l) {
+        const SSchedule &S = M->level[l];
+        std::unordered_map<long long, int> ridx;          // T offset -> reduce index of the level
+        for (size_t i = 0; i < S.reduces.size(); ++i) ridx[S.reduces[i].t] = (int)i;
+        SSchedule &CS = M->capsched[l];
+        CS.tile_m = tc2::M;
+        for (const CapItem &c : F->lv[l].n.caps) {
+            const auto i1 = ridx.find(c.t1), i2 = ridx.find(c.t2);
+            if (c.r1 != tc2::M || c.r2 != tc2::M || i1 == ridx.end() || i2 == ridx.end()) {
+                M->capfb[l].push_back(c);
+                continue;
+            }
+            kj.push_back(RSliceJob{c.k, kel, 2 * tc2::M, 2 * tc2::M, 2 * tc2::M, 2 * tc2::M / 16, kexp});
+            kb.push_back(krows);
+            krows += 2 * tc2::M;
+            for (int t = 0; t < 2; ++t) {
+                CS.tile_row0.push_back((int)(t == 0 ? c.t1 : c.t2));
+                CS.tile_begin.push_back((int)CS.xterms.size());
+                const long long a = kel + (long long)t * 16 * kTbA;
+                CS.xterms.push_back(XTerm{a, S.reduces[i1->second].tpad, tc2::M, kexp + t * tc2::M, 0, i1->second});
+                CS.xterms.push_back(XTerm{a + 8 * kTbA, S.reduces[i2->second].tpad, tc2::M, kexp + t * tc2::M, 0,
+                                          i2->second});
+            }
+            kel += 2LL * 16 * kTbA;
+            kexp += 2 * tc2::M;
+        }
+        CS.tile_begin.push_back((int)CS.xterms.size());
+        if ((rc = upload_tb(CS, &M->bytes))) return rc;
+        if ((rc = dev_vec(M->capfb[l], &M->d_capfb[l], &M->bytes))) return rc;
+    }
+    if (kj.empty()) return 0;
+    M->kstride = al32(kel);
+    if (cudaMalloc((void **)&M->kslices, (size_t)kNS * M->kstride * sizeof(bf16)) != cudaSuccess)
+        return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate capacitance slices");
+    M->bytes += (long long)kNS * M->kstride * 2;
+    if ((rc = dev_vec(std::vector<int>(kexp, 0), &M->kexps, &M->bytes))) return rc;
+    RSliceJob *d_kj = nullptr;
+    int *d_kb = nullptr;
+    long long tmp = 0;
+    if ((rc = dev_vec(kj, &d_kj, &tmp)) || (rc = dev_vec(kb, &d_kb, &tmp))) return rc;
+    slice_r_tb_kernel<kNS><<<(krows + 127) / 128, 128, 0, st>>>(d_kj, d_kb, (int)kj.size(), krows, F->kpool,
+                                                               M->kslices, M->kstride, M->kexps);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_kj);
+    cudaFree(d_kb);
+    if (e != cudaSuccess) return fail(DPLR_GPU_ECUDA, "capacitance slicing: %s", cudaGetErrorString(e));
+    return tb_attrs<kNS, kD>();
+}
+
 template <int NS>
 static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
 {
@@ -2262,6 +2339,7 @@ static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
         S.t_per_rhs = p->total_rank;
         if ((rc = upload_tb(S, &M->bytes))) return rc;
     }
+    if (M->tc_caps && (rc = build_tc_caps(p, M, F, st))) return rc;
     SSchedule &LS = M->leaf;
     LS.tile_m = tc2::M;
     for (size_t i = 0; i < p->leaves.size(); ++i) {
@@ -2298,7 +2376,12 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
     const long long wstride = M->tpad_per_rhs * njt;
     const size_t ws_bytes = r256((size_t)NS * wstride * sizeof(bf16));
     const size_t we_bytes = r256(maxred * nrhs * sizeof(int));
-    const size_t need = part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes;
+    // tensor-core capacitance: T in 8 slices and their exponents
+    const bool tcc = M->tc_caps && M->kslices;
+    const long long tstride8 = M->tpad_per_rhs * njt;
+    const size_t t8_bytes = tcc ? r256((size_t)kNS * tstride8 * sizeof(bf16)) : 0;
+    const size_t te8_bytes = tcc ? r256(maxred * nrhs * sizeof(int)) : 0;
+    const size_t need = part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes + t8_bytes + te8_bytes;
     if (M->work_bytes < need) {
         cudaFree(M->work);
         M->work = nullptr;
@@ -2313,6 +2396,8 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
     double *W = reinterpret_cast<double *>(base + part_bytes + t_bytes);
     bf16 *ws = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes + w_bytes);
     int *wexp = reinterpret_cast<int *>(base + part_bytes + t_bytes + w_bytes + ws_bytes);
+    bf16 *ts8 = reinterpret_cast<bf16 *>(base + part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes);
+    int *texp8 = reinterpret_cast<int *>(base + part_bytes + t_bytes + w_bytes + ws_bytes + we_bytes + t8_bytes);
     const double npairs = pair_count(NS, D);
     int rc;
 
@@ -2374,7 +2459,27 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
             launch_reduce<D>(S, partials, M->exps, M->xexp, p->pool, nrhs, T, lo_off, st);
             DG_CUDA(cudaGetLastError());
         }
-        if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
+        if (tcc && !M->capsched[l].xterms.empty()) {
+            // W = K^-1 [T1; T2] on the tensor cores for the rank-128 nodes
+            {
+                ProfScope ps("mixed_tslice", st, 0.0, 0.0);
+                tslice_tb_kernel<kNS><<<dim3((unsigned)S.reduces.size(), (unsigned)njt), 256, 0, st>>>(
+                    S.d_reduces, (int)S.reduces.size(), T, lo_off, nrhs, njt, ts8, tstride8, texp8);
+                note_launch();
+            }
+            {
+                const SSchedule &CS = M->capsched[l];
+                const double fc = 2.0 * tc2::M * tc2::M * nrhs * (double)CS.xterms.size() * pair_count(kNS, kD);
+                ProfScope ps("capacitance_tc", st, fc, 0.0);
+                launch_expand_tb<kNS, kD>(p, CS, M->kslices, M->kstride, M->kexps, ts8, tstride8, texp8, M->xs, m,
+                                          M->xexp, nrhs, false, nullptr, 0, false, W, tc2::M, st, nullptr, nullptr,
+                                          nullptr, nrhs);
+                DG_CUDA(cudaGetLastError());
+            }
+            if ((rc = run_cap_list(M->capfb[l], M->d_capfb[l], F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
+        } else if ((rc = run_caps(F->lv[l].n, F->kpool, nullptr, 0, T, W, nrhs, st))) {
+            return rc;
+        }
         {
             ProfScope ps("mixed_tslice", st, 0.0, 0.0);
             tslice_tb_kernel<NS><<<dim3((unsigned)S.reduces.size(), (unsigned)njt), 256, 0, st>>>(

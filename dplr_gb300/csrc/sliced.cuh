@@ -140,12 +140,22 @@ struct MixedSliced {
     size_t xexp_n = 0;
     int *xexp2 = nullptr;          // exponents of the X being written (swapped with xexp)
     size_t xexp2_n = 0;
+    // Capacitance on the tensor cores: the K^-1 of every node with two
+    // rank-128 blocks in 8 exact slices (row exponents), applied by the
+    // multi-term expand; other nodes keep the FP64 kernel.
+    bool tc_caps = false;
+    bf16 *kslices = nullptr;
+    long long kstride = 0;
+    int *kexps = nullptr;
+    std::vector<SSchedule> capsched;             // per level: output tiles of K^-1 [T1; T2]
+    std::vector<std::vector<CapItem>> capfb;     // per level: nodes left to the FP64 kernel
+    std::vector<CapItem *> d_capfb;
     void *work = nullptr;
     size_t work_bytes = 0;
     long long bytes = 0;
 };
 
-int mixed_build(Plan *p, int ns, cudaStream_t st);
+int mixed_build(Plan *p, int ns, cudaStream_t st, bool fp64_caps = false);
 void mixed_free(Plan *p);
 // X = A^-1 B with the low-precision sweep (B and X must not alias).
 int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx, cudaStream_t st);

@@ -106,9 +106,14 @@ int dplr_gpu_prepare_sliced(dplr_gpu_plan plan, void *stream)
 
 int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream)
 {
+    return dplr_gpu_prepare_mixed_caps(plan, slices, 0, stream);
+}
+
+int dplr_gpu_prepare_mixed_caps(dplr_gpu_plan plan, int slices, int fp64_capacitance, void *stream)
+{
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_mixed: null plan");
-    return mixed_build(p, slices, (cudaStream_t)stream);
+    return mixed_build(p, slices, (cudaStream_t)stream, fp64_capacitance != 0);
 }
 
 int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *B, int ldb,

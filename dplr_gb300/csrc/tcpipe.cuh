@@ -338,6 +338,8 @@ __device__ __forceinline__ int nkb_of(int K) { return (K + KB - 1) / KB; }
 
 // Y[tile, 64 columns] = (-1)^neg sum_terms A_t B_t (+ Bin).  Work item
 // it = tile * njt + jt (right-hand-side tiles of one row tile adjacent).
+// Output row i of a tile is Y row tile_row0 * rscale + i (rscale > 1 places
+// tiles at offsets that scale with the right-hand-side count).
 // LEAN (D <= 8, every tile a single term, as in the inner solve): the
 // product of each output is one 64-bit integer, rounded once to FP64 and
 // added to Bin in FP64 (accurate far beyond the inner solve's slices); otherwise
@@ -350,7 +352,7 @@ __global__ void __maxnreg__(kRegs)
                   const int *__restrict__ texp, const bf16 *__restrict__ xs, long long xstride, int xnjt,
                   const int *__restrict__ xexp, int nrhs, int neg, const double *__restrict__ Bin, int ldbin,
                   int addb, double *__restrict__ Y, int ldy, const int *__restrict__ rmaxt,
-                  const int *__restrict__ cmaxt, int *__restrict__ yexp, int *err)
+                  const int *__restrict__ cmaxt, int *__restrict__ yexp, int rscale, int *err)
 {
     using C = Cfg<NS>;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -448,7 +450,7 @@ __global__ void __maxnreg__(kRegs)
             for (int it = blockIdx.x; it < nitems && !ctl.abort; it += gridDim.x) {
                 const int tile = it / njt, jt = it % njt;
                 const int j0 = jt * N + ch * CPW;
-                const int gr = tile_row0[tile] + row;
+                const long long gr = (long long)tile_row0[tile] * rscale + row;
                 double bv[CPW];
                 if (addb) {
 #pragma unroll
@@ -572,7 +574,7 @@ __global__ void __maxnreg__(kRegs)
             }
             if (!ok) break;
             // outputs: fold in +-Bin exactly, round once
-            const int gr = tile_row0[tile] + row;
+            const long long gr = (long long)tile_row0[tile] * rscale + row;
 #pragma unroll
             for (int c = 0; c < CPW; ++c) {
                 const int j = j0 + c;

@@ -97,10 +97,12 @@ class GpuPlan:
                                                       ctypes.byref(nb), ctypes.byref(ms)), "dplr_gpu_autotune")
         return {"chunk_rows": c.value, "nb_cap": nb.value, "apply_ms": ms.value}
 
-    def prepare_mixed(self, slices: int = 7, stream=None) -> None:
-        """Sliced factor copies (3 to 7 bf16 slices) for the low-precision inner solve."""
-        _native.check(_native.lib().dplr_gpu_prepare_mixed(self._h, int(slices), _stream_ptr(stream)),
-                      "dplr_gpu_prepare_mixed")
+    def prepare_mixed(self, slices: int = 7, fp64_capacitance: bool = False, stream=None) -> None:
+        """Sliced factor copies (3 to 7 bf16 slices) for the low-precision inner
+        solve; the capacitance inverses apply from 8 exact slices on the tensor
+        cores (rank-128 nodes) unless fp64_capacitance."""
+        _native.check(_native.lib().dplr_gpu_prepare_mixed_caps(self._h, int(slices), int(bool(fp64_capacitance)),
+                                                               _stream_ptr(stream)), "dplr_gpu_prepare_mixed")
         self.mixed = True
         self.mixed_slices = int(slices)
 

@@ -109,11 +109,18 @@ DPLR_API int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int l
 
 /* Low-precision inner solver for refinement: the Woodbury sweep with V,
  * the D^-1 W panels and the leaf inverses cut into `slices` bf16 slices
- * (3 to 7: 22 to 50 bits) on the tensor cores, capacitance inverses
- * applied in FP64.  More slices cost more tensor-core work per solve but
- * keep the refinement convergent on worse-conditioned factorisations.
- * Needs dplr_gpu_factor first and leaf sizes that are multiples of 64. */
+ * (3 to 7: 22 to 50 bits) on the tensor cores.  The capacitance inverses
+ * are formed and stored in FP64; nodes whose two blocks have rank 128 (with
+ * 128-row tiles) apply them on the tensor cores from 8 exact slices (57-bit
+ * operands, exact products, one rounding: at least FP64 accuracy), the
+ * others with FP64 arithmetic.  More slices cost more tensor-core work per
+ * solve but keep the refinement convergent on worse-conditioned
+ * factorisations.  Needs dplr_gpu_factor first and leaf sizes that are
+ * multiples of 64. */
 DPLR_API int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream);
+/* Same, with fp64_capacitance != 0 applying every capacitance inverse with
+ * FP64 arithmetic. */
+DPLR_API int dplr_gpu_prepare_mixed_caps(dplr_gpu_plan plan, int slices, int fp64_capacitance, void *stream);
 
 /* X := A^-1 B refined until max_j ||B_j - A X_j|| / ||B_j|| <= tol; at
  * most maxiter corrections.  flags: DPLR_GPU_RESIDUAL_SLICED selects the

@@ -217,3 +217,30 @@ def test_seventh_slice_shrinks_inner_solve_error():
         _, res[ns], _ = p.solve_refined(b, tol=1e-30, maxiter=0, precise=True, mixed=True, strict=False)
         p.close()
     assert res[6] < res[5] / 20 and res[7] < res[6] / 20, res
+
+
+def test_tensor_core_capacitance_matches_fp64():
+    """Nodes with two rank-128 blocks apply K^-1 from 8 exact slices on the
+    tensor cores; the refined solves with it and with FP64 capacitance both
+    reach the tolerance and agree, and one unrefined inner solve is as
+    accurate either way."""
+    from dplr_gb300 import gen_gpu
+    from dplr_gb300.plan import GpuPlan
+    t = gen_gpu.kernel_tree_2d(n=16384, leaf=128, rmax=128, seed=6)
+    assert max(tree.ranks_by_level(t)) == 128
+    g = torch.Generator(device="cpu").manual_seed(4)
+    b = torch.randn(70, t.size, generator=g, dtype=torch.float64).cuda()
+    out = {}
+    for fp64 in (False, True):
+        p = GpuPlan(t)
+        p.factor()
+        p.prepare_sliced()
+        p.prepare_mixed(7, fp64_capacitance=fp64)
+        _, r0, _ = p.solve_refined(b, tol=1e-30, maxiter=0, precise=True, mixed=True, strict=False)
+        x, r, _ = p.solve_refined(b, tol=1e-12, maxiter=10, precise=True, mixed=True)
+        out[fp64] = (x, r, r0)
+        p.close()
+    (xt, rt, r0t), (xf, rf, r0f) = out[False], out[True]
+    assert rt <= 1e-12 and rf <= 1e-12, (rt, rf)
+    assert float(((xt - xf).norm(dim=1) / xf.norm(dim=1)).max()) <= 1e-9
+    assert r0t <= 4 * r0f and r0f <= 4 * r0t, (r0t, r0f)
