@@ -382,6 +382,51 @@ __global__ void __launch_bounds__(kThreads) cap_kernel(
     }
 }
 
+// Capacitance of small nodes (order r <= 64): one CTA per (node, 64
+// right-hand sides); thread (i, g) owns row i and the 16 columns of group g,
+// [T1; T2] for the 64 columns staged in shared memory.  Same arithmetic as
+// cap_kernel (one FMA chain per output over k), with every thread busy.
+__global__ void __launch_bounds__(kThreads) cap_small_kernel(
+    const CapItem *__restrict__ items, const double *__restrict__ kbase,
+    const double *__restrict__ sigbase, int trans, int scaled, const double *__restrict__ T,
+    double *__restrict__ W, int nrhs)
+{
+    __shared__ double Ts[64][65];
+    const CapItem c = items[blockIdx.x];
+    const int r = c.r1 + c.r2;
+    const int j0 = blockIdx.y * 64;
+    const int nj = min(64, nrhs - j0);
+    const double *K = kbase + c.k;
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        const int k = e % 64, j = e / 64;
+        double v = 0.0;
+        if (k < r && j < nj)
+            v = k < c.r1 ? T[c.t1 * nrhs + k + (long long)(j0 + j) * c.r1]
+                         : T[c.t2 * nrhs + (k - c.r1) + (long long)(j0 + j) * c.r2];
+        Ts[j][k] = v;
+    }
+    __syncthreads();
+    const int i = threadIdx.x & 63, g = threadIdx.x >> 6;
+    if (i >= r) return;
+    double acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = 0.0;
+    for (int k = 0; k < r; ++k) {
+        const double a = trans ? K[k + (long long)i * r] : K[i + (long long)k * r];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) acc[u] = fma(a, Ts[g * 16 + u][k], acc[u]);
+    }
+    double s = 1.0;
+    if (scaled) s = i < c.r1 ? sigbase[c.s1 + i] : sigbase[c.s2 + i - c.r1];
+    for (int u = 0; u < 16; ++u) {
+        const int j = g * 16 + u;
+        if (j >= nj) break;
+        double *w = i < c.r1 ? W + c.t1 * nrhs + i + (long long)(j0 + j) * c.r1
+                             : W + c.t2 * nrhs + (i - c.r1) + (long long)(j0 + j) * c.r2;
+        *w = s * acc[u];
+    }
+}
+
 // ------------------------------------------------------------- utilities
 __global__ void scale_kernel(double *Y, int rows, int cols, int ldy, double beta)
 {
@@ -536,6 +581,8 @@ int run_cap_list(const std::vector<CapItem> &caps, const CapItem *d_caps, const 
     const int nb = std::min(pick_nb(nrhs), 8);
     dim3 g((unsigned)caps.size(), (unsigned)((nrhs + nb - 1) / nb));
     const int scaled = sigbase != nullptr;
+    int rmax = 0;
+    for (const CapItem &c : caps) rmax = std::max(rmax, c.r1 + c.r2);
     double fl = 0, by = 0;
     for (const CapItem &c : caps) {
         double r = c.r1 + c.r2;
@@ -544,6 +591,12 @@ int run_cap_list(const std::vector<CapItem> &caps, const CapItem *d_caps, const 
     }
     ProfScope ps("capacitance", st, fl, by);
     note_launch();
+    if (rmax <= 64 && nrhs >= 16) {
+        cap_small_kernel<<<dim3((unsigned)caps.size(), (unsigned)((nrhs + 63) / 64)), kThreads, 0, st>>>(
+            d_caps, kbase, sigbase, trans, scaled, T, W, nrhs);
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
     switch (nb) {
     case 8: cap_kernel<8><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
     case 4: cap_kernel<4><<<g, kThreads, 0, st>>>(d_caps, kbase, sigbase, trans, scaled, T, W, nrhs); break;
