@@ -43,8 +43,8 @@ struct PairScratch {
     double *w = nullptr;         // partials and T (FP64)
     int *ex = nullptr;           // exponent of max |x| (device)
     size_t t_n = 0, w_n = 0;     // capacities of t and w (the schedule may change after prepare)
-    // output tiles of the expand: R rows (up to 256, one thread per row), so
-    // every factor column is read in 2 KB contiguous pieces
+    // output tiles of the expand: R rows (64, or the largest power of two
+    // dividing every leaf); 256 threads = R rows x 256/R inner-index groups
     int R = 0;
     std::vector<int> row0, begin;
     std::vector<TileTerm> terms;
@@ -334,7 +334,7 @@ int pairs_prepare(Plan *p, cudaStream_t st)
     if (rc) return bail(rc);
     int g = 0;
     for (const LeafDesc &L : p->leaves) g = std::gcd(g, L.b);
-    P->R = kPThreads;
+    P->R = 64;            // 64-row tiles: 4x the CTAs of 256-row ones, same bandwidth at full size
     while (P->R > 1 && g > 0 && g % P->R != 0) P->R >>= 1;
     build_tiles(p, 0, P->R, P->row0, P->begin, P->terms);
     auto up = [&](auto &v, auto **d) -> int {
