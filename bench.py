@@ -41,7 +41,7 @@ METRIC = ("PLR solve RHS/s @N=2^18,256 RHS: mixed+refined vs FP64 GPU at ≤1e-1
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1 << 18)
@@ -86,7 +86,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -261,6 +261,9 @@ def run_reference(args):
         return
     t, stats = build_matrix(args, device=dev)
     threads = os.cpu_count() or 1
+    warm = max(0, args.warmup)
+    for _ in range(warm):                     # untimed samples (caches, thread pools)
+        cpu_sample(t, args, threads)
     steps = []
     for _ in range(max(1, args.steps)):
         steps.append(cpu_sample(t, args, threads))
@@ -272,7 +275,7 @@ def run_reference(args):
               f"solve flops (2*nnz(inv)+2*nnz(A) per refinement step)")
     out = {
         "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": 1, "steps": len(steps),
-        "warmup": 0, "ms_per_step": 1000.0 * args.rhs / value if value else None,
+        "warmup": warm, "ms_per_step": 1000.0 * args.rhs / value if value else None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
         "config": workload_config(args, stats, {"parallelism": "host cores"}),
