@@ -482,16 +482,17 @@ __global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items, int nite
 {
     const long long E = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (E >= total) return;
-    const long long q = E / nrhs;
+    // the item (binary search by multiplication) and the element within it
+    // (one 32-bit division: rank * nrhs of one item stays below 2^31)
     int lo = 0, hi = nitems - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (items[mid].rsum <= q) lo = mid; else hi = mid - 1;
+        if ((long long)items[mid].rsum * nrhs <= E) lo = mid; else hi = mid - 1;
     }
     const SReduceItem R = items[lo];
     const long long cnt = (long long)R.rank * nrhs;
-    const long long e = E - (long long)R.rsum * nrhs;
-    const int k = (int)(e % R.rank), j = (int)(e / R.rank);
+    const int e = (int)(E - (long long)R.rsum * nrhs);
+    const int j = e / R.rank, k = e - j * R.rank;
     const __int128 *P = partials + R.p * nrhs + e;
     __int128 W0 = 0, W1 = 0, W2 = 0, W3 = 0;
     int c = 0;
