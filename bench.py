@@ -57,7 +57,7 @@ def parse():
                     help="bf16 slices of the mixed inner solve (3 to 7)")
     ap.add_argument("--residual", choices=["sliced", "fp64"], default="sliced",
                     help="refinement residual: exact-slice tensor-core products or the FP64 apply")
-    ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint"], default="solve",
+    ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint", "compress"], default="solve",
                     help="solve: the headline refined solve; the others are secondary workloads "
                          "(dplr_gb300/workloads.py)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -530,12 +530,15 @@ def run_secondary(args):
     elif args.workload == "batched":
         sampler.start()
         out = workloads.batched_workload(max(args.steps, 10), args.warmup)
+    elif args.workload == "compress":
+        sampler.start()
+        out = workloads.compress_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
     else:
         sampler.start()
         out = workloads.adjoint_workload(max(args.steps, 5), args.warmup)
     out["clocks"] = sampler.stop()
-    out.update({"n_gpus": 1, "steps": max(args.steps, 10), "warmup": max(3, args.warmup), "scaling": "weak",
-                "vs_baseline": None, "data": "synthetic"})
+    out.update({"n_gpus": 1, "steps": out.pop("steps", max(args.steps, 10)), "warmup": max(3, args.warmup),
+                "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
     if rank == 0:
         print(json.dumps(out))
 

@@ -39,6 +39,7 @@ _SIGNATURES = {
     "scal": (None, [c_int, POINTER(c_double), PDPlrMtx]),
     "axpy": (None, [c_int, POINTER(c_double), PDPlrMtx, PDPlrMtx]),
     "adpy": (None, [c_int, POINTER(c_double), c_double_p, PDPlrMtx]),
+    "d2gep": (None, [c_int, c_double_p, c_int, PDPlrMtx, c_double, c_int, POINTER(c_int)]),
 }
 
 
@@ -118,3 +119,11 @@ class PlrApi:
 
     def adpy(self, m: int, alpha: float, d: np.ndarray, b) -> None:
         self.fn["adpy"](m, ctypes.byref(c_double(alpha)), _ptr(d), b)
+
+    # dense -> PLR compression ---------------------------------------------
+    def d2gep(self, m: int, a: np.ndarray, lda: int, b, eps: float, nlvl: int) -> int:
+        """a: the column-major dense matrix, flat or 2-D Fortran-ordered."""
+        info = c_int(-12345)
+        flat = a.reshape(-1, order="F") if a.ndim == 2 else a
+        self.fn["d2gep"](m, _ptr(flat), lda, b, eps, nlvl, ctypes.byref(info))
+        return info.value

@@ -18,6 +18,13 @@
   refactorisation (the factors change between steps of an optimisation),
   solve, transposed solve, factor gradient.
 
+* ``compress``: dense -> PLR compression (dplrd2gep) of the 2D Gaussian
+  kernel matrix of 4096 points (2-D uniform, cluster-sorted), 4 levels,
+  eps = 1e-8; one step is one host-to-host call (A copied in, the tree
+  copied out).  The CPU legs restate the same compression with LAPACK on
+  the host cores: dgesvd (the reference's SVD) timed on one half-tree and
+  one top-level block, and gesdd (numpy) on the whole matrix.
+
 Each returns the JSON record of its line; the caller adds clocks.
 """
 from __future__ import annotations
@@ -29,7 +36,7 @@ import time
 import numpy as np
 import torch
 
-from . import _native, gen
+from . import _native, gen, tree
 from .plan import GpuGraph, GpuPlan
 
 
@@ -238,3 +245,110 @@ def adjoint_workload(steps: int, warmup: int, n: int = 65536) -> dict:
                                "transposed solve and factor gradient per step",
                    "pool_doubles": plan.pool_size(), "loss": float(loss), "fd_check": fd},
     }
+
+
+def gauss2d_dense(m: int, seed: int = 0, width: float = 0.05, shift: float = 1e-3) -> np.ndarray:
+    """exp(-|p_i - p_j|^2 / width) + shift I for m uniform points in the unit
+    square, sorted into 16 x 16 cells so that index blocks are clusters."""
+    pts = np.random.default_rng(seed).random((m, 2))
+    pts = pts[np.argsort(np.floor(pts[:, 0] * 16) * 16 + pts[:, 1])]
+    d2 = ((pts[:, None, :] - pts[None, :, :]) ** 2).sum(-1)
+    return np.exp(-d2 / width) + shift * np.eye(m)
+
+
+def _lapack_compress(a: np.ndarray, eps: float, nlvl: int, driver: str):
+    """The compression of src/dplrd2p.c:186 on the host with one LAPACK SVD
+    driver; returns the ranks in DPLR's order."""
+    import scipy.linalg as sl
+    ranks = []
+
+    def rec(blk, e, lv):
+        if lv == 0:
+            return
+        e2 = e / 2.0 if lv == 1 else e / 4.0
+        h = blk.shape[0] // 2
+        for off in (blk[:h, h:], blk[h:, :h]):
+            s = sl.svd(off, full_matrices=False, compute_uv=True, lapack_driver=driver)[1]
+            ranks.append(int(np.argmax(s < e2)) if np.any(s < e2) else len(s))
+        rec(blk[:h, :h], e2, lv - 1)
+        rec(blk[h:, h:], e2, lv - 1)
+
+    rec(a, eps, nlvl)
+    return ranks
+
+
+def compress_workload(steps: int, warmup: int, m: int = 4096, nlvl: int = 4, eps: float = 1e-8,
+                      cpu: bool = True) -> dict:
+    from .compress import d2gep
+    a = np.asfortranarray(gauss2d_dense(m))
+    times = {}
+    for workers in (1, 0):
+        for _ in range(max(3, warmup) if workers == 0 else 1):
+            t = d2gep(a, eps, nlvl, workers)
+        torch.cuda.synchronize()
+        k = steps if workers == 0 else max(1, steps // 3)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            t = d2gep(a, eps, nlvl, workers)
+        times[workers] = (time.perf_counter() - t0) / k
+    ranks = tree.ranks_by_level(t)
+    out_bytes = 8 * _stored(t)
+    sec = times[0]
+    rec = {
+        "metric": f"dense->PLR compressions/s (dplrd2gep, N={m}, {nlvl} levels, eps={eps:g})",
+        "value": 1.0 / sec, "unit": "compressions/s", "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "dtype": "f64", "gpu_launches": 0, "steps": steps,
+        "e2e": {"value": 1.0 / sec, "unit": "compressions/s", "h2d_bytes_per_step": 8 * m * m,
+                "d2h_bytes_per_step": out_bytes},
+        "config": {"workload": f"2D Gaussian kernel, {m} uniform points in the unit square (width 0.05, "
+                               f"shift 1e-3), {nlvl} levels, eps {eps:g}; host A in, host tree out; "
+                               "SVDs by cuSOLVER gesvd (library kernels)",
+                   "ms_one_worker": times[1] * 1e3, "ms_default_workers": sec * 1e3,
+                   "max_rank_by_level": ranks},
+    }
+    if cpu:
+        import scipy.linalg as sl
+        h = m // 2
+        eh = eps / 4.0                       # the threshold handed to each half
+        t0 = time.perf_counter()
+        half = _lapack_compress(a[:h, :h], eh, nlvl - 1, "gesvd")
+        t_half = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sl.svd(a[:h, h:], full_matrices=False, lapack_driver="gesvd")
+        t_top = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dd = _lapack_compress(a, eps, nlvl, "gesdd")
+        t_dd = time.perf_counter() - t0
+        est = 2 * t_top + 2 * t_half
+        rec["cpu_baseline"] = {
+            "value": 1.0 / est, "unit": "compressions/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"LAPACK dgesvd (the reference's SVD, scipy/OpenBLAS, all host threads): one "
+                       f"half-tree ({h}, {nlvl - 1} levels) {t_half:.2f} s and one top-level block "
+                       f"{t_top:.2f} s timed; whole compression = 2 x both")}
+        rec["config"]["cpu_gesdd_s"] = t_dd
+        rec["config"]["ranks_match_gesdd"] = dd == _ranks_all(t)
+        rec["config"]["half_ranks_match"] = half == _ranks_all(t.nw)
+    return rec
+
+
+def _stored(t) -> int:
+    """Doubles held by the tree: n^2 per leaf, (2 n + 1) r per low-rank block."""
+    if isinstance(t, tree.HNode):
+        return sum(_stored(c) for c in (t.nw, t.ne, t.se, t.sw))
+    if isinstance(t, tree.LowRank):
+        return (2 * t.size + 1) * t.rank
+    return t.size * t.size
+
+
+def _ranks_all(t) -> list:
+    """Low-rank block ranks in DPLR's depth-first NE, SW, NW, SE order."""
+    out = []
+
+    def walk(nd):
+        if isinstance(nd, tree.HNode):
+            out.extend([nd.ne.rank, nd.sw.rank])
+            walk(nd.nw)
+            walk(nd.se)
+
+    walk(t)
+    return out

@@ -163,6 +163,15 @@ DPLR_API void dplrgeinv(int m, DPlrMtx *A, DPlrMtx *B, double eps, int *info);
  * Gram-Schmidt routine src/dortlr.f90:12 fixed (see dplr_gb300.h). */
 DPLR_API void dplrreduce(int m, DPlrMtx *A, double eps);
 
+/* Compress the dense m x m matrix A (lda >= m) into the PLR matrix B with
+ * nlvl levels and absolute accuracy eps; each off-diagonal block is a
+ * truncated SVD computed on the GPU (cuSOLVER gesvd), the threshold eps/2
+ * on the last level and eps/4 above it.  B is rebuilt where its type or
+ * size differs.  info = 0 on success, -1 on invalid arguments, the SVD's
+ * info if it does not converge.  Replaces dplrd2gep, src/dplrd2p.c:186. */
+DPLR_API void dplrd2gep(int m, double *A, int lda, DPlrMtx *B, double eps,
+               int nlvl, int *info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -229,6 +229,14 @@ DPLR_API int dplr_gpu_profile_stop(void);
 DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double *flops,
                                     double *bytes, int *launches);
 
+/* dplrd2gep with the number of SVD workers chosen (each a host thread with
+ * its own stream, cuSOLVER handle and buffers; 0 = 8, fewer where device
+ * memory is short).  dplrd2gep is this call with workers = 0.  Returns
+ * DPLR_GPU_EINVAL on invalid arguments, DPLR_GPU_ECUDA on a CUDA or
+ * cuSOLVER error, else DPLR_GPU_OK with DPLR's info in *info. */
+DPLR_API int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int nlvl,
+                            int workers, int *info);
+
 /* Associate the drop-in entry points with a plan for this host tree
  * (they then skip the upload).  dplr_gpu_unregister drops the link. */
 DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);
