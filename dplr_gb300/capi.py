@@ -40,6 +40,8 @@ _SIGNATURES = {
     "axpy": (None, [c_int, POINTER(c_double), PDPlrMtx, PDPlrMtx]),
     "adpy": (None, [c_int, POINTER(c_double), c_double_p, PDPlrMtx]),
     "d2gep": (None, [c_int, c_double_p, c_int, PDPlrMtx, c_double, c_int, POINTER(c_int)]),
+    "geppmm": (None, [c_char, c_char, c_int, POINTER(c_double), PDPlrMtx, PDPlrMtx,
+                      POINTER(c_double), PDPlrMtx, c_double]),
 }
 
 
@@ -119,6 +121,11 @@ class PlrApi:
 
     def adpy(self, m: int, alpha: float, d: np.ndarray, b) -> None:
         self.fn["adpy"](m, ctypes.byref(c_double(alpha)), _ptr(d), b)
+
+    def geppmm(self, transa: str, transb: str, m: int, alpha: float, a, b, beta: float, c,
+               eps: float) -> None:
+        self.fn["geppmm"](transa.encode(), transb.encode(), m, ctypes.byref(c_double(alpha)), a, b,
+                          ctypes.byref(c_double(beta)), c, eps)
 
     # dense -> PLR compression ---------------------------------------------
     def d2gep(self, m: int, a: np.ndarray, lda: int, b, eps: float, nlvl: int) -> int:

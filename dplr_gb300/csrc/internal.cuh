@@ -177,7 +177,10 @@ int validate_tree(int m, const DPlrMtx *A, const char *fn);
 // schedule helpers (plan.cu)
 int tile_rows_for(const Plan *p);
 void build_tiles(const Plan *p, int trans, int R, std::vector<int> &row0, std::vector<int> &begin,
-                 std::vector<TileTerm> &terms);
+                 std::vector<TileTerm> &terms, int lmin = 0);
+// Apply schedule (op N: trans 0, op T: trans 1) of the blocks of H nodes at
+// depth >= lmin and every leaf.
+void build_schedule(const Plan *p, int trans, Schedule &S, int lmin = 0);
 int upload_schedule(Schedule &S, long long *bytes);
 void free_schedule(Schedule &S);
 

@@ -160,14 +160,17 @@ int tile_rows_for(const Plan *p)
 // block's output rows plus the leaf term.
 // Output tiles of R rows (R divides every leaf) and their terms: every
 // low-rank block whose output rows cover the tile, then the leaf term.
+// Blocks of H nodes shallower than lmin are left out: the schedule then
+// applies the block-diagonal part of the matrix made of its subtrees at
+// depth lmin (and the leaves above them).
 void build_tiles(const Plan *p, int trans, int R, std::vector<int> &row0, std::vector<int> &begin,
-                 std::vector<TileTerm> &terms)
+                 std::vector<TileTerm> &terms, int lmin)
 {
     int ntiles = p->m / R;
     std::vector<std::vector<TileTerm>> per(ntiles);
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
-        if (L.rank == 0) continue;
+        if (L.rank == 0 || L.level < lmin) continue;
         int out0 = trans ? L.col0 : L.row0;
         long long base = trans ? L.v : L.u;
         for (int t0 = out0; t0 < out0 + L.n; t0 += R) {
@@ -213,7 +216,7 @@ void build_tiles(const Plan *p, int trans, int R, std::vector<int> &row0, std::v
     begin.push_back((int)terms.size());
 }
 
-static void build_schedule(Plan *p, int trans, Schedule &S)
+void build_schedule(const Plan *p, int trans, Schedule &S, int lmin)
 {
     const int CH = p->chunk_rows;
     S.items.clear();
@@ -221,7 +224,7 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
     long long poff = 0;
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
-        if (L.rank == 0 || L.n == 0) continue;
+        if (L.rank == 0 || L.n == 0 || L.level < lmin) continue;
         int nch = (L.n + CH - 1) / CH;
         for (int c = 0; c < nch; ++c) {
             PanelItem it;
@@ -249,7 +252,7 @@ static void build_schedule(Plan *p, int trans, Schedule &S)
     S.max_rank = p->max_rank;
 
     S.tile_rows = tile_rows_for(p);
-    build_tiles(p, trans, S.tile_rows, S.tile_row0, S.tile_begin, S.terms);
+    build_tiles(p, trans, S.tile_rows, S.tile_row0, S.tile_begin, S.terms, lmin);
 }
 
 template <class T>

@@ -158,6 +158,14 @@ DPLR_API void dplrgeprk(int m, int k, double *alpha, double *u, int ldu,
  * src/dplrinv.c:93. */
 DPLR_API void dplrgeinv(int m, DPlrMtx *A, DPlrMtx *B, double eps, int *info);
 
+/* C := alpha*op(A)*op(B) + beta*C for PLR matrices of one structure; the
+ * low-rank blocks of C grow by the products' columns (normalised, zeroed
+ * below eps/4 per level), nothing is recompressed.  Replaces dplrgeppmm,
+ * src/dplrppmm.c:998. */
+DPLR_API void dplrgeppmm(char transa, char transb, int m, double *alpha,
+                DPlrMtx *A, DPlrMtx *B, double *beta, DPlrMtx *C,
+                double eps);
+
 /* Re-orthogonalise and truncate every low-rank block (eps/4 per level).
  * Replaces dplrreduce, src/dplrreduce.c:25, with the interface of the
  * Gram-Schmidt routine src/dortlr.f90:12 fixed (see dplr_gb300.h). */

@@ -237,6 +237,13 @@ DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double
 DPLR_API int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int nlvl,
                             int workers, int *info);
 
+/* dplrgeppmm with a status: DPLR_GPU_EINVAL (message in
+ * dplr_gpu_last_error) when A, B and C differ in structure or are
+ * malformed, before C is touched; DPLR_GPU_ECUDA / DPLR_GPU_ENOMEM on a
+ * device error.  stream: the CUDA stream of the device work. */
+DPLR_API int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlrMtx *A, DPlrMtx *B,
+                             double beta, DPlrMtx *C, double eps, void *stream);
+
 /* Associate the drop-in entry points with a plan for this host tree
  * (they then skip the upload).  dplr_gpu_unregister drops the link. */
 DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);
