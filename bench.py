@@ -57,7 +57,8 @@ def parse():
                     help="bf16 slices of the mixed inner solve (3 to 7)")
     ap.add_argument("--residual", choices=["sliced", "fp64"], default="sliced",
                     help="refinement residual: exact-slice tensor-core products or the FP64 apply")
-    ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint", "compress"], default="solve",
+    ap.add_argument("--workload", choices=["solve", "apply", "batched", "adjoint", "compress", "ppmm"],
+                    default="solve",
                     help="solve: the headline refined solve; the others are secondary workloads "
                          "(dplr_gb300/workloads.py)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -530,6 +531,9 @@ def run_secondary(args):
     elif args.workload == "batched":
         sampler.start()
         out = workloads.batched_workload(max(args.steps, 10), args.warmup)
+    elif args.workload == "ppmm":
+        sampler.start()
+        out = workloads.ppmm_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
     elif args.workload == "compress":
         sampler.start()
         out = workloads.compress_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)

@@ -34,9 +34,13 @@
 #include "internal.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 namespace dg {
@@ -54,15 +58,24 @@ struct GemmJob {
     double alpha, beta;
 };
 
+// Output tile (i0, j0) of a job over k in [k0, k1); p >= 0: raw partial sums
+// to part + p (ld M), summed in slice order by gemm_reduce_kernel (split K
+// for long, skinny products).
 struct GemmTile {
-    int job, i0, j0;
+    int job, i0, j0, k0, k1;
+    long long p;
+};
+
+struct GemmRed {
+    long long p;
+    int job, slices;
 };
 
 constexpr int kGT = 64;   // output tile edge
 constexpr int kGK = 16;   // k step staged in shared memory
 
 __global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ jobs,
-                                                   const GemmTile *__restrict__ tiles)
+                                                   const GemmTile *__restrict__ tiles, double *__restrict__ part)
 {
     const GemmTile t = tiles[blockIdx.x];
     const GemmJob J = jobs[t.job];
@@ -74,14 +87,14 @@ __global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ j
     for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
-    for (int k0 = 0; k0 < J.K; k0 += kGK) {
+    for (int k0 = t.k0; k0 < t.k1; k0 += kGK) {
         for (int e = threadIdx.x; e < kGT * kGK; e += 256) {
             // consecutive threads walk the contiguous index of the operand
             const int i = J.ta ? e / kGK : e % kGT;
             const int k = J.ta ? e % kGK : e / kGT;
             const int gi = t.i0 + i, gk = k0 + k;
             double v = 0.0;
-            if (gi < J.M && gk < J.K) {
+            if (gi < J.M && gk < t.k1) {
                 v = J.ta ? J.a[gk + (long long)gi * J.lda] : J.a[gi + (long long)gk * J.lda];
                 if (J.ks) v *= J.ks[gk];
             }
@@ -92,7 +105,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ j
             const int k = J.tb ? e / kGT : e % kGK;
             const int gj = t.j0 + j, gk = k0 + k;
             double v = 0.0;
-            if (gj < J.N && gk < J.K)
+            if (gj < J.N && gk < t.k1)
                 v = J.tb ? J.b[gj + (long long)gk * J.ldb] : J.b[gk + (long long)gj * J.ldb];
             Bs[k][j] = v;
         }
@@ -116,12 +129,31 @@ __global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ j
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const int i = t.i0 + ty + 16 * r, j = t.j0 + tx + 16 * c;
-            if (i < J.M && j < J.N) {
+            if (i < J.M && j < J.N && t.p >= 0) {
+                part[t.p + i + (long long)j * J.M] = acc[r][c];
+            } else if (i < J.M && j < J.N) {
                 double v = J.alpha * acc[r][c];
                 if (J.beta != 0.0) v = fma(J.beta, J.c[i + (long long)j * J.ldc], v);
                 J.d[i + (long long)j * J.ldd] = v;
             }
         }
+}
+
+// D = alpha * (sum of a split job's slices, in order) + beta C.
+__global__ void gemm_reduce_kernel(const GemmJob *__restrict__ jobs, const GemmRed *__restrict__ reds,
+                                   const double *__restrict__ part)
+{
+    const GemmRed R = reds[blockIdx.y];
+    const GemmJob J = jobs[R.job];
+    const long long mn = (long long)J.M * J.N;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < mn; e += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int q = 0; q < R.slices; ++q) acc += part[R.p + q * mn + e];
+        const int i = (int)(e % J.M), j = (int)(e / J.M);
+        double v = J.alpha * acc;
+        if (J.beta != 0.0) v = fma(J.beta, J.c[i + (long long)j * J.ldc], v);
+        J.d[i + (long long)j * J.ldd] = v;
+    }
 }
 
 // One column pair of C (or one side of a term), built from its sources.
@@ -203,15 +235,19 @@ __global__ void copy_kernel(const CopyJob *__restrict__ jobs, const int2 *__rest
 
 // ---------------------------------------------------------- host side --
 
+// Device memory of one call, stream-ordered (cudaMallocAsync), released
+// after the call's work.
 struct Arena {
+    cudaStream_t st;
     std::vector<void *> ptrs;
+    explicit Arena(cudaStream_t s) : st(s) {}
     ~Arena()
     {
-        for (void *p : ptrs) cudaFree(p);
+        for (void *p : ptrs) cudaFreeAsync(p, st);
     }
     template <class T> int alloc(T **p, long long n)
     {
-        if (cudaMalloc((void **)p, (size_t)std::max<long long>(n, 1) * sizeof(T)) != cudaSuccess)
+        if (cudaMallocAsync((void **)p, (size_t)std::max<long long>(n, 1) * sizeof(T), st) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "dplrgeppmm: cannot allocate %lld bytes", n * (long long)sizeof(T));
         ptrs.push_back(*p);
         return 0;
@@ -220,7 +256,7 @@ struct Arena {
     {
         int rc = alloc(p, (long long)v.size());
         if (rc) return rc;
-        if (!v.empty()) DG_CUDA(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) DG_CUDA(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
         return 0;
     }
 };
@@ -229,17 +265,42 @@ int launch_gemms(Arena &ar, const std::vector<GemmJob> &jobs, cudaStream_t st)
 {
     if (jobs.empty()) return 0;
     std::vector<GemmTile> tiles;
-    for (int j = 0; j < (int)jobs.size(); ++j)
-        for (int i0 = 0; i0 < jobs[j].M; i0 += kGT)
-            for (int j0 = 0; j0 < jobs[j].N; j0 += kGT) tiles.push_back({j, i0, j0});
+    std::vector<GemmRed> reds;
+    long long ptot = 0;
+    for (int j = 0; j < (int)jobs.size(); ++j) {
+        const GemmJob &J = jobs[j];
+        const int mt = (J.M + kGT - 1) / kGT, nt = (J.N + kGT - 1) / kGT;
+        // long, skinny products: split K into slices of >= 512
+        int slices = 1;
+        if (mt * nt <= 4 && J.K >= 1024) slices = std::min(64, J.K / 512);
+        const int chunk = ((J.K + slices - 1) / slices + kGK - 1) / kGK * kGK;
+        slices = J.K > 0 ? (J.K + chunk - 1) / chunk : 1;
+        const long long p = slices > 1 ? ptot : -1;
+        for (int q = 0; q < slices; ++q)
+            for (int i0 = 0; i0 < J.M; i0 += kGT)
+                for (int j0 = 0; j0 < J.N; j0 += kGT)
+                    tiles.push_back({j, i0, j0, q * chunk, std::min(J.K, (q + 1) * chunk),
+                                     p < 0 ? -1 : p + (long long)q * J.M * J.N});
+        if (slices > 1) {
+            reds.push_back({p, j, slices});
+            ptot += (long long)slices * J.M * J.N;
+        }
+    }
     if (tiles.empty()) return 0;
     GemmJob *dj;
     GemmTile *dt;
+    GemmRed *dr = nullptr;
+    double *part = nullptr;
     int rc;
     if ((rc = ar.upload(jobs, &dj)) || (rc = ar.upload(tiles, &dt))) return rc;
+    if (!reds.empty() && ((rc = ar.upload(reds, &dr)) || (rc = ar.alloc(&part, ptot)))) return rc;
     for (size_t b0 = 0; b0 < tiles.size(); b0 += 1u << 30) {
         const unsigned nb = (unsigned)std::min<size_t>(tiles.size() - b0, 1u << 30);
-        gemm_kernel<<<nb, 256, 0, st>>>(dj, dt + b0);
+        gemm_kernel<<<nb, 256, 0, st>>>(dj, dt + b0, part);
+        note_launch();
+    }
+    if (!reds.empty()) {
+        gemm_reduce_kernel<<<dim3(16, (unsigned)reds.size()), 256, 0, st>>>(dj, dr, part);
         note_launch();
     }
     DG_CUDA(cudaGetLastError());
@@ -275,6 +336,20 @@ int launch_copies(Arena &ar, const std::vector<CopyJob> &jobs, const std::vector
     note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
+}
+
+// Pinned host staging of the result, kept between calls and grown on
+// demand (dplr_gpu_release_staging frees it).
+struct Staging {
+    std::mutex mu;
+    double *p = nullptr;
+    size_t n = 0;
+};
+
+Staging &staging()
+{
+    static Staging s;
+    return s;
 }
 
 // op(M)'s view of a low-rank block: u-side, v-side, singular values.
@@ -347,17 +422,20 @@ int restricted_apply(Arena &ar, const Plan *p, int trans, int lmin, const double
 {
     Schedule S;
     build_schedule(p, trans, S, lmin);
-    long long bytes = 0;
-    int rc = upload_schedule(S, &bytes);
+    for (const PanelItem &it : S.items) S.max_len = std::max(S.max_len, it.len);
+    for (const TileTerm &t : S.terms) S.has_row_major = S.has_row_major || t.trans_a;
     double *T = nullptr, *partials = nullptr;
-    if (!rc) rc = ar.alloc(&T, std::max<long long>(1, S.t_per_rhs * nrhs));
-    if (!rc) rc = ar.alloc(&partials, std::max<long long>(1, S.partial_per_rhs * nrhs));
-    if (!rc) rc = run_panel(S, p->pool, X, p->m, nrhs, partials, st);
-    if (!rc) rc = run_reduce(S, p->pool, partials, nrhs, T, st);
-    if (!rc) rc = run_expand(S, p->pool, T, X, p->m, Y, p->m, nrhs, alpha, 0.0, st);
-    if (!rc) rc = cudaStreamSynchronize(st) == cudaSuccess ? 0 : fail(DPLR_GPU_ECUDA, "dplrgeppmm: apply failed");
-    free_schedule(S);
-    return rc;
+    int rc;
+    if ((rc = ar.upload(S.items, &S.d_items)) || (rc = ar.upload(S.reduces, &S.d_reduces)) ||
+        (rc = ar.upload(S.tile_row0, &S.d_tile_row0)) || (rc = ar.upload(S.tile_begin, &S.d_tile_begin)) ||
+        (rc = ar.upload(S.terms, &S.d_terms)))
+        return rc;
+    if ((rc = ar.alloc(&T, std::max<long long>(1, S.t_per_rhs * nrhs))) ||
+        (rc = ar.alloc(&partials, std::max<long long>(1, S.partial_per_rhs * nrhs))))
+        return rc;
+    if ((rc = run_panel(S, p->pool, X, p->m, nrhs, partials, st))) return rc;
+    if ((rc = run_reduce(S, p->pool, partials, nrhs, T, st))) return rc;
+    return run_expand(S, p->pool, T, X, p->m, Y, p->m, nrhs, alpha, 0.0, st);
 }
 
 int geppmm_device(int ta, int tb, int m, double alpha, const DPlrMtx *A, const DPlrMtx *B, double beta, DPlrMtx *C,
@@ -365,12 +443,13 @@ int geppmm_device(int ta, int tb, int m, double alpha, const DPlrMtx *A, const D
 {
     PlanSet ps;
     int rc;
-    if ((rc = plan_build(m, A, st, &ps.a)) || (rc = plan_build(m, B, st, &ps.b)) || (rc = plan_build(m, C, st, &ps.c)))
+    if ((rc = plan_build(m, A, st, &ps.a)) || (B != A && (rc = plan_build(m, B, st, &ps.b))) ||
+        (rc = plan_build(m, C, st, &ps.c)))
         return rc;
-    const Plan *pa = ps.a, *pb = ps.b, *pc = ps.c;
+    const Plan *pa = ps.a, *pb = B != A ? ps.b : ps.a, *pc = ps.c;
     const std::vector<HDesc> &nodes = pc->nodes;
     const int nH = (int)nodes.size(), nL = (int)pc->leaves.size();
-    Arena ar;
+    Arena ar(st);
 
     // thresholds of dplrppmm's recursion: eps/4 per level
     std::vector<double> e2(nH);
@@ -638,13 +717,39 @@ int geppmm_device(int ta, int tb, int m, double alpha, const DPlrMtx *A, const D
     }
     for (const std::vector<GemmJob> &jobs : by_dist)
         if ((rc = launch_gemms(ar, jobs, st))) return rc;
-    DG_CUDA(cudaStreamSynchronize(st));
 
     // ---- host: DPLR's capacity growth, then the values
-    std::vector<double> host((size_t)tot);
-    DG_CUDA(cudaMemcpy(host.data(), out, sizeof(double) * (size_t)tot, cudaMemcpyDeviceToHost));
+    // Grown blocks get fresh buffers (live columns from the device, the rest
+    // NaN as dplrresizelr leaves it).  The result comes back in one copy to
+    // pinned staging and is spread to the tree's buffers by host threads.
+    Staging &sg = staging();
+    std::lock_guard<std::mutex> lk(sg.mu);
+    if (sg.n < (size_t)tot) {
+        if (sg.p) cudaFreeHost(sg.p);
+        sg.p = nullptr;
+        sg.n = 0;
+        const size_t want = std::max<size_t>((size_t)tot, (size_t)tot + (size_t)tot / 2);
+        DG_CUDA(cudaMallocHost((void **)&sg.p, sizeof(double) * want));
+        sg.n = want;
+    }
+    DG_CUDA(cudaMemcpyAsync(sg.p, out, sizeof(double) * (size_t)tot, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    struct Piece {
+        size_t src;            // offset in the result (doubles); SIZE_MAX: NaN fill
+        double *dst;
+        size_t count;
+    };
+    std::vector<Piece> pieces;
+    const double qnan = std::nan("");
+    const size_t kNaN = (size_t)-1;
+    auto add = [&](size_t src, double *dst, size_t count) {
+        // at most 256 K doubles per piece, so that threads share big blocks
+        for (size_t o = 0; o < count; o += (1u << 18))
+            pieces.push_back({src == kNaN ? kNaN : src + o, dst + o, std::min<size_t>(1u << 18, count - o)});
+    };
     for (int b = 0; b < nb; ++b) {
         DPlrMtx *L = lrs[b];
+        // dplrresizelr at every append that overflows, in DPLR's order
         int cap = L->dlr.capacity, r = 0;
         bool first = true;
         for (const Segment &g : segs[b]) {
@@ -656,20 +761,54 @@ int geppmm_device(int ta, int tb, int m, double alpha, const DPlrMtx *A, const D
             }
             first = false;
         }
-        if (cap > L->dlr.capacity) dplrresizelr(L, cap);
-        if (L->dlr.capacity < rank_f[b]) return fail(DPLR_GPU_ENOMEM, "dplrgeppmm: capacity growth failed");
         const size_t n = (size_t)L->size, rf = (size_t)rank_f[b];
+        if (cap > L->dlr.capacity) {
+            double *u = (double *)malloc(sizeof(double) * n * cap);
+            double *v = (double *)malloc(sizeof(double) * n * cap);
+            double *sg = (double *)malloc(sizeof(double) * cap);
+            if (!u || !v || !sg) {
+                free(u);
+                free(v);
+                free(sg);
+                return fail(DPLR_GPU_ENOMEM, "dplrgeppmm: host allocation failed");
+            }
+            free(L->dlr.u);
+            free(L->dlr.v);
+            free(L->dlr.sig);
+            L->dlr.u = u;
+            L->dlr.v = v;
+            L->dlr.sig = sg;
+            L->dlr.capacity = cap;
+            add(kNaN, u + n * rf, n * (cap - rf));
+            add(kNaN, v + n * rf, n * (cap - rf));
+            add(kNaN, sg + rf, cap - rf);
+        }
         if (rf) {
-            memcpy(L->dlr.u, host.data() + off_u[b], sizeof(double) * n * rf);
-            memcpy(L->dlr.v, host.data() + off_v[b], sizeof(double) * n * rf);
-            memcpy(L->dlr.sig, host.data() + off_s[b], sizeof(double) * rf);
+            add((size_t)off_u[b], L->dlr.u, n * rf);
+            add((size_t)off_v[b], L->dlr.v, n * rf);
+            add((size_t)off_s[b], L->dlr.sig, rf);
         }
         L->dlr.rank = (int)rf;
     }
     for (int l = 0; l < nL; ++l) {
         const size_t bl = (size_t)pc->leaves[l].b;
-        if (bl) memcpy(leaves[l]->dd.d, host.data() + off_d[l], sizeof(double) * bl * bl);
+        if (bl) add((size_t)off_d[l], leaves[l]->dd.d, bl * bl);
     }
+    const double *stage = sg.p;
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i = next.fetch_add(1); i < pieces.size(); i = next.fetch_add(1)) {
+            const Piece &q = pieces[i];
+            if (q.src == kNaN) std::fill(q.dst, q.dst + q.count, qnan);
+            else memcpy(q.dst, stage + q.src, sizeof(double) * q.count);
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = (unsigned)std::min<size_t>(std::min(16u, hw), std::max<size_t>(1, pieces.size() / 4));
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; ++t) th.emplace_back(worker);
+    worker();
+    for (std::thread &t : th) t.join();
     return 0;
 }
 
@@ -701,6 +840,15 @@ int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlrMtx *A, D
     if ((rc = same_structure(A, B, C, fn))) return rc;
     if (m == 0) return 0;
     return geppmm_device(ta, tb, m, alpha, A, B, beta, C, eps, (cudaStream_t)stream);
+}
+
+void dplr_gpu_release_staging(void)
+{
+    Staging &sg = staging();
+    std::lock_guard<std::mutex> lk(sg.mu);
+    if (sg.p) cudaFreeHost(sg.p);
+    sg.p = nullptr;
+    sg.n = 0;
 }
 
 void dplrgeppmm(char transa, char transb, int m, double *alpha, DPlrMtx *A, DPlrMtx *B, double *beta, DPlrMtx *C,

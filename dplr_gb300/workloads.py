@@ -25,6 +25,13 @@
   the host cores: dgesvd (the reference's SVD) timed on one half-tree and
   one top-level block, and gesdd (numpy) on the whole matrix.
 
+* ``ppmm``: the PLR x PLR product C := A A + 0.5 C (dplrgeppmm) on the 2D
+  Gaussian-kernel matrix of the solve benchmark at N = 16384 (leaf 256,
+  ranks up to 64), eps = 1e-8; one step is one host-to-host call (A and C
+  uploaded, C's grown tree copied back).  The CPU leg is the restatement
+  oracle/ppmm.py (the reference's recursion, numpy BLAS on all host
+  threads) on the same inputs; its result is the parity check.
+
 Each returns the JSON record of its line; the caller adds clocks.
 """
 from __future__ import annotations
@@ -352,3 +359,80 @@ def _ranks_all(t) -> list:
 
     walk(t)
     return out
+
+
+def _max_rel_diff(a, b) -> float:
+    """Largest difference of two trees of one structure, relative to the
+    largest entry of the node it occurs in; inf if structures, ranks or
+    capacities differ."""
+    if type(a) is not type(b) or a.size != b.size:
+        return float("inf")
+    if isinstance(a, tree.HNode):
+        return max(_max_rel_diff(getattr(a, k), getattr(b, k)) for k in ("nw", "ne", "se", "sw"))
+    if isinstance(a, tree.LowRank):
+        if a.rank != b.rank or a.capacity != b.capacity:
+            return float("inf")
+        pairs = [(a.u, b.u), (a.v, b.v), (a.sig, b.sig)]
+    else:
+        pairs = [(a.d, b.d)]
+    out = 0.0
+    for x, y in pairs:
+        if y.size:
+            out = max(out, float(np.abs(x - y).max()) / max(1.0, float(np.abs(y).max())))
+    return out
+
+
+def ppmm_workload(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax: int = 64,
+                  eps: float = 1e-8, cpu: bool = True) -> dict:
+    import copy
+    import ctypes
+    from . import gen_gpu
+    t = gen_gpu.kernel_tree_2d(n=n, leaf=leaf, rmax=rmax, seed=0, device="cuda")
+    lib = _native.lib()
+    ca = tree.to_c(t)
+    nw = max(3, warmup)
+    cs = [tree.to_c(t) for _ in range(nw + steps)]
+    try:
+        def call(c):
+            rc = lib.dplr_gpu_geppmm(b"N", b"N", n, 1.0, ca, ca, 0.5, c, eps, None)
+            _native.check(rc, "dplr_gpu_geppmm")
+
+        for i in range(nw):
+            call(cs[i])
+        torch.cuda.synchronize()
+        l0 = _native.launch_count()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            call(cs[nw + i])
+        sec = (time.perf_counter() - t0) / steps
+        launches = (_native.launch_count() - l0) // steps
+        got = tree.from_c(cs[-1])
+    finally:
+        tree.free_c(ca)
+        for c in cs:
+            tree.free_c(c)
+    h2d = 8 * (2 * tree.nnz(t) + 2 * n)          # A and C (two copies of the matrix)
+    d2h = 8 * _stored(got)
+    rec = {
+        "metric": f"PLR x PLR products/s (dplrgeppmm C := A A + 0.5 C, N={n}, host trees in and out)",
+        "value": 1.0 / sec, "unit": "products/s", "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "dtype": "f64", "gpu_launches": launches, "steps": steps,
+        "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "config": {"workload": f"2D Gaussian kernel PLR, N={n}, leaf {leaf}, ranks up to {rmax}; "
+                               f"C := A A + 0.5 C with eps {eps:g}",
+                   "ranks_in": tree.ranks_by_level(t), "ranks_out": tree.ranks_by_level(got),
+                   "stored_doubles_in": _stored(t), "stored_doubles_out": _stored(got)},
+    }
+    if cpu:
+        import os
+        from oracle import ppmm as oppmm
+        c = copy.deepcopy(t)
+        t0 = time.perf_counter()
+        oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, eps)
+        cpu_s = time.perf_counter() - t0
+        rec["cpu_baseline"] = {
+            "value": 1.0 / cpu_s, "unit": "products/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"one whole product by the restatement of src/dplrppmm.c (oracle/ppmm.py, numpy BLAS "
+                      f"on all host threads): {cpu_s:.2f} s"}
+        rec["config"]["max_rel_diff_vs_cpu"] = _max_rel_diff(got, c)
+    return rec

@@ -243,6 +243,9 @@ DPLR_API int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double 
  * device error.  stream: the CUDA stream of the device work. */
 DPLR_API int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlrMtx *A, DPlrMtx *B,
                              double beta, DPlrMtx *C, double eps, void *stream);
+/* dplrgeppmm returns its result through a pinned host buffer that is kept
+ * (at 1.5x the largest result so far) for later calls; this frees it. */
+DPLR_API void dplr_gpu_release_staging(void);
 
 /* Associate the drop-in entry points with a plan for this host tree
  * (they then skip the upload).  dplr_gpu_unregister drops the link. */
