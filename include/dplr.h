@@ -16,9 +16,10 @@
  *     `rank` columns are live.  V is stored as V, not V^T;
  *   - ne maps x[m/2:m] to y[0:m/2]; sw maps x[0:m/2] to y[m/2:m].
  *
- * The apply and inverse routines (dplrgepmv, dplrgepdmm, dplrgeinv,
- * dplrgeprk, dplrreduce) run on the GPU; the structural helpers run on
- * the host.  GPU-specific additions live in dplr_gb300.h.
+ * The apply, inverse, product and compression routines (dplrgepmv,
+ * dplrgepdmm, dplrgeinv, dplrgeprk, dplrgeppmm, dplrreduce, dplrd2gep) run
+ * on the GPU; the structural helpers run on the host.  GPU-specific
+ * additions live in dplr_gb300.h.
  */
 #ifndef DPLR_GB300_DPLR_H
 #define DPLR_GB300_DPLR_H
