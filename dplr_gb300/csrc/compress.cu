@@ -14,7 +14,13 @@
 // worker threads, each with its own stream, cuSOLVER handle and buffers:
 // the SVD (cuSOLVER's gesvd, the QR-iteration SVD LAPACK's dgesvd is) of a
 // small block is a long chain of small launches, so independent blocks run
-// side by side.  The tree B stays on the host, as DPLR's callers expect.
+// side by side.  Blocks of 512 and more first try a sketch: Q = orth(A
+// Omega) (own Gaussian and FP64 GEMM kernels, cuSOLVER QR), B = Q^T A and
+// the residual ||A - Q B||_F; when the residual proves that no singular
+// value at or above the threshold is missed and the kept ones are as
+// accurate as a full SVD's, the SVD of the n x l matrix B^T gives the
+// block's factors, otherwise the full SVD runs.  The tree B stays on the
+// host, as DPLR's callers expect.
 // Argument checks, messages and info codes are DPLR's: info = -1 on invalid
 // arguments, the SVD's info if one does not converge.
 #include <cuda_runtime.h>
@@ -30,10 +36,16 @@
 
 #include "../../include/dplr.h"
 #include "../../include/dplr_gb300.h"
+#include "gemm.cuh"
 
 namespace dg {
 int fail(int code, const char *fmt, ...);
+void note_launch();
+void note_launches(long long k);
 }
+using dg::GemmJob;
+using dg::GemmRed;
+using dg::GemmTile;
 
 namespace {
 
@@ -52,6 +64,10 @@ struct Solver {
     decltype(&cusolverDnSetStream) set_stream = nullptr;
     decltype(&cusolverDnDgesvd_bufferSize) gesvd_size = nullptr;
     decltype(&cusolverDnDgesvd) gesvd = nullptr;
+    decltype(&cusolverDnDgeqrf_bufferSize) geqrf_size = nullptr;
+    decltype(&cusolverDnDgeqrf) geqrf = nullptr;
+    decltype(&cusolverDnDorgqr_bufferSize) orgqr_size = nullptr;
+    decltype(&cusolverDnDorgqr) orgqr = nullptr;
     bool ok = false;
 
     Solver()
@@ -65,7 +81,11 @@ struct Solver {
         set_stream = (decltype(set_stream))dlsym(so, "cusolverDnSetStream");
         gesvd_size = (decltype(gesvd_size))dlsym(so, "cusolverDnDgesvd_bufferSize");
         gesvd = (decltype(gesvd))dlsym(so, "cusolverDnDgesvd");
-        ok = create && destroy && set_stream && gesvd_size && gesvd;
+        geqrf_size = (decltype(geqrf_size))dlsym(so, "cusolverDnDgeqrf_bufferSize");
+        geqrf = (decltype(geqrf))dlsym(so, "cusolverDnDgeqrf");
+        orgqr_size = (decltype(orgqr_size))dlsym(so, "cusolverDnDorgqr_bufferSize");
+        orgqr = (decltype(orgqr))dlsym(so, "cusolverDnDorgqr");
+        ok = create && destroy && set_stream && gesvd_size && gesvd && geqrf_size && geqrf && orgqr_size && orgqr;
     }
 };
 
@@ -74,6 +94,51 @@ const Solver &solver()
     static const Solver s;
     return s;
 }
+
+// Standard normal sketch entries from a counter-based hash (SplitMix64
+// finaliser) and the Box-Muller transform: deterministic per (seed, index).
+__device__ inline unsigned long long mix64(unsigned long long z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void gauss_kernel(double *out, long long count, unsigned long long seed)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long h = mix64(seed ^ mix64((unsigned long long)i));
+        const double u1 = ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);        // (0, 1)
+        const double u2 = (double)(mix64(h) >> 11) * (1.0 / 9007199254740992.0);         // [0, 1)
+        out[i] = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    }
+}
+
+// Sum of squares of a rows x cols block (ld lda): one partial per CTA.
+__global__ void fro2_kernel(const double *a, int lda, int rows, int cols, double *part)
+{
+    __shared__ double red[8];
+    double q = 0.0;
+    const long long cnt = (long long)rows * cols;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (long long)gridDim.x * blockDim.x) {
+        const double x = a[(e % rows) + (e / rows) * (long long)lda];
+        q = fma(x, x, q);
+    }
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+constexpr int kFroBlocks = 128;   // partials of fro2_kernel
+constexpr int kRandMin = 512;     // blocks at least this large try the sketch first
 
 // One off-diagonal block: rows r0.., columns c0.. of A, order n.
 struct Job {
@@ -115,37 +180,167 @@ struct Worker {
     cudaStream_t st = nullptr;
     cusolverDnHandle_t h = nullptr;
     double *W = nullptr, *U = nullptr, *VT = nullptr, *S = nullptr, *work = nullptr, *rwork = nullptr;
+    // sketch path: Omega / U of A, Q, B^T, U of B^T (n x lmax), V^T of B^T
+    // (lmax x lmax), Householder scalars, norm partials
+    double *Om = nullptr, *Q = nullptr, *Bt = nullptr, *Ub = nullptr, *Vbt = nullptr, *tau = nullptr, *fro = nullptr;
     int *info = nullptr;
-    int lwork = 0;
+    int lwork = 0, lmax = 0;
     std::vector<double> hS, hVT;
 
     bool init(int nmax)
     {
         const size_t nn = (size_t)nmax * nmax;
+        lmax = nmax >= kRandMin ? nmax / 3 : 0;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return false;
         if (solver().create(&h) != CUSOLVER_STATUS_SUCCESS) return false;
         if (solver().set_stream(h, st) != CUSOLVER_STATUS_SUCCESS) return false;
         if (solver().gesvd_size(h, nmax, nmax, &lwork) != CUSOLVER_STATUS_SUCCESS) return false;
+        if (lmax > 0) {
+            int a = 0, b = 0, c = 0;
+            if (solver().geqrf_size(h, nmax, lmax, W, nmax, &a) != CUSOLVER_STATUS_SUCCESS ||
+                solver().orgqr_size(h, nmax, lmax, lmax, W, nmax, S, &b) != CUSOLVER_STATUS_SUCCESS ||
+                solver().gesvd_size(h, nmax, lmax, &c) != CUSOLVER_STATUS_SUCCESS)
+                return false;
+            lwork = std::max({lwork, a, b, c});
+        }
+        const size_t nl = (size_t)nmax * std::max(lmax, 1), ll = (size_t)std::max(lmax, 1) * std::max(lmax, 1);
         return cudaMalloc((void **)&W, nn * sizeof(double)) == cudaSuccess &&
                cudaMalloc((void **)&U, nn * sizeof(double)) == cudaSuccess &&
                cudaMalloc((void **)&VT, nn * sizeof(double)) == cudaSuccess &&
                cudaMalloc((void **)&S, (size_t)nmax * sizeof(double)) == cudaSuccess &&
                cudaMalloc((void **)&rwork, (size_t)nmax * sizeof(double)) == cudaSuccess &&
                cudaMalloc((void **)&work, (size_t)std::max(lwork, 1) * sizeof(double)) == cudaSuccess &&
-               cudaMalloc((void **)&info, sizeof(int)) == cudaSuccess;
+               cudaMalloc((void **)&info, sizeof(int)) == cudaSuccess &&
+               cudaMalloc((void **)&Om, nl * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&Q, nl * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&Bt, nl * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&Ub, nl * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&Vbt, ll * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&tau, (size_t)std::max(lmax, 1) * sizeof(double)) == cudaSuccess &&
+               cudaMalloc((void **)&fro, 2 * kFroBlocks * sizeof(double)) == cudaSuccess;
     }
 
     void release()
     {
-        cudaFree(W);
-        cudaFree(U);
-        cudaFree(VT);
-        cudaFree(S);
-        cudaFree(work);
-        cudaFree(rwork);
+        for (double *p : {W, U, VT, S, work, rwork, Om, Q, Bt, Ub, Vbt, tau, fro}) cudaFree(p);
         cudaFree(info);
         if (h) solver().destroy(h);
         if (st) cudaStreamDestroy(st);
+    }
+
+    // One GEMM on the worker's stream (tables staged in stream-ordered memory).
+    bool gemm(const GemmJob &J)
+    {
+        std::vector<GemmJob> jobs{J};
+        std::vector<GemmTile> tiles;
+        std::vector<GemmRed> reds;
+        long long ptot = 0;
+        plan_gemm_tiles(jobs, tiles, reds, ptot);
+        if (tiles.empty()) return true;
+        GemmJob *dj = nullptr;
+        GemmTile *dt = nullptr;
+        GemmRed *dr = nullptr;
+        double *part = nullptr;
+        bool ok = cudaMallocAsync((void **)&dj, sizeof(GemmJob), st) == cudaSuccess &&
+                  cudaMallocAsync((void **)&dt, sizeof(GemmTile) * tiles.size(), st) == cudaSuccess &&
+                  cudaMemcpyAsync(dj, jobs.data(), sizeof(GemmJob), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+                  cudaMemcpyAsync(dt, tiles.data(), sizeof(GemmTile) * tiles.size(), cudaMemcpyHostToDevice, st) ==
+                      cudaSuccess;
+        if (ok && !reds.empty())
+            ok = cudaMallocAsync((void **)&dr, sizeof(GemmRed) * reds.size(), st) == cudaSuccess &&
+                 cudaMallocAsync((void **)&part, sizeof(double) * ptot, st) == cudaSuccess &&
+                 cudaMemcpyAsync(dr, reds.data(), sizeof(GemmRed) * reds.size(), cudaMemcpyHostToDevice, st) ==
+                     cudaSuccess;
+        if (ok) {
+            run_gemm_tables(dj, dt, tiles.size(), dr, reds.size(), part, st);
+            dg::note_launches((long long)((tiles.size() + (1u << 30) - 1) >> 30) + (reds.empty() ? 0 : 1));
+            ok = cudaGetLastError() == cudaSuccess;
+        }
+        for (void *q : {(void *)dj, (void *)dt, (void *)dr, (void *)part})
+            if (q) cudaFreeAsync(q, st);
+        return ok;
+    }
+
+    // Frobenius norm of a rows x cols block (ld lda); < 0 on error.
+    double fro_norm(const double *a, int lda, int rows, int cols)
+    {
+        fro2_kernel<<<kFroBlocks, 256, 0, st>>>(a, lda, rows, cols, fro);
+        dg::note_launch();
+        double hp[kFroBlocks];
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(hp, fro, sizeof(hp), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return -1.0;
+        double t = 0.0;
+        for (double x : hp) t += x;
+        return sqrt(t);
+    }
+
+    // Sketch path for a large block: Q = orth(A Omega), B^T = A^T Q, checked
+    // by the residual ||A - Q B||_F; on success the SVD of B^T (n x l) gives
+    // A's leading singular triplets (A ~ (Q V_b) S U_b^T).  Accepted only when
+    // the residual is below 1e-3 of the threshold, or at rounding level
+    // (32 eps ||A||_F) and below half the threshold: then no singular value
+    // at or above the threshold is missed (sigma_{l+1}(A) <= ||A - Q B||) and
+    // the kept ones are as accurate as a full SVD's.  Returns 0 (done), 2 (not
+    // accepted: use the full SVD), -1 on an error.
+    int run_sketch(const double *dA, int m, Job &jb)
+    {
+        const int n = jb.n;
+        const double *Ab = dA + jb.r0 + (size_t)jb.c0 * m;
+        const double fa = fro_norm(Ab, m, n, n);
+        if (fa < 0) return -1;
+        const unsigned long long seed = ((unsigned long long)jb.r0 << 32) ^ (unsigned long long)jb.c0;
+        const int lcap = std::min(lmax, n / 3);   // beyond n/3 columns the full SVD is as cheap
+        for (int l = std::min(192, lcap); l >= 32 && l <= lcap; l = (l == lcap ? lcap + 1 : std::min(2 * l, lcap))) {
+            gauss_kernel<<<256, 256, 0, st>>>(Om, (long long)n * l, seed + (unsigned long long)l);
+            dg::note_launch();
+            if (cudaGetLastError() != cudaSuccess) return -1;
+            // Q = orth(A Omega)
+            if (!gemm({Ab, Om, nullptr, nullptr, Q, n, l, n, m, n, 0, n, 0, 0, 1.0, 0.0})) return -1;
+            if (solver().geqrf(h, n, l, Q, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS ||
+                solver().orgqr(h, n, l, l, Q, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS)
+                return -1;
+            // B^T = A^T Q ; W = A - Q B
+            if (!gemm({Ab, Q, nullptr, nullptr, Bt, n, l, n, m, n, 0, n, 1, 0, 1.0, 0.0})) return -1;
+            if (cudaMemcpy2DAsync(W, (size_t)n * sizeof(double), Ab, (size_t)m * sizeof(double),
+                                  (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return -1;
+            if (!gemm({Q, Bt, W, nullptr, W, n, n, l, n, n, n, n, 0, 1, -1.0, 1.0})) return -1;
+            const double fe = fro_norm(W, n, n, n);
+            if (fe < 0) return -1;
+            const double eps64 = 2.220446049250313e-16;
+            const bool accept = fe <= 1e-3 * jb.eps || (fe <= 32.0 * eps64 * fa && fe < 0.5 * jb.eps);
+            if (!accept) continue;
+            // B^T = U_b S V_b^T
+            if (solver().gesvd(h, 'S', 'S', n, l, Bt, n, S, Ub, n, Vbt, l, work, lwork, rwork, info) !=
+                CUSOLVER_STATUS_SUCCESS)
+                return -1;
+            int devinfo = 0;
+            hS.resize(l);
+            if (cudaMemcpyAsync(&devinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaMemcpyAsync(hS.data(), S, (size_t)l * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return -1;
+            if (devinfo != 0) return 2;
+            int rank = 0;
+            while (rank < l && !(hS[rank] < jb.eps)) ++rank;
+            DPlrMtx *L = jb.L;
+            if (L->dlr.capacity < rank) dplrresizelr(L, rank);
+            L->dlr.rank = rank;
+            if (rank == 0) return 0;
+            memcpy(L->dlr.sig, hS.data(), (size_t)rank * sizeof(double));
+            // U = Q V_b (first rank columns) into Om ; V = U_b
+            if (!gemm({Q, Vbt, nullptr, nullptr, Om, n, rank, l, n, l, 0, n, 0, 1, 1.0, 0.0})) return -1;
+            if (cudaMemcpyAsync(L->dlr.u, Om, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaMemcpyAsync(L->dlr.v, Ub, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return -1;
+            return 0;
+        }
+        return 2;
     }
 
     // Truncated SVD of one block (dplrlrappx, src/dplrd2p.c:22): 0, the
@@ -157,6 +352,10 @@ struct Worker {
         if (n == 0) {
             L->dlr.rank = 0;
             return 0;
+        }
+        if (n >= kRandMin && lmax >= 32) {
+            const int rs = run_sketch(dA, m, jb);
+            if (rs != 2) return rs;
         }
         if (cudaMemcpy2DAsync(W, (size_t)n * sizeof(double), dA + jb.r0 + (size_t)jb.c0 * m, (size_t)m * sizeof(double),
                               (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)

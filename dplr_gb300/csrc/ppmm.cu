@@ -32,6 +32,7 @@
 // order) on C and stores the columns, so ranks, capacities and column
 // order are DPLR's.
 #include "internal.cuh"
+#include "gemm.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -48,113 +49,6 @@ namespace dg {
 namespace {
 
 // ------------------------------------------------------------ kernels --
-
-// D = alpha op(A) diag(ks) op(B) + beta C  (C not read when beta == 0; C
-// may be D).  op(A) is M x K: a[i + k lda] (ta = 0) or a[k + i lda].
-struct GemmJob {
-    const double *a, *b, *c, *ks;
-    double *d;
-    int M, N, K, lda, ldb, ldc, ldd, ta, tb;
-    double alpha, beta;
-};
-
-// Output tile (i0, j0) of a job over k in [k0, k1); p >= 0: raw partial sums
-// to part + p (ld M), summed in slice order by gemm_reduce_kernel (split K
-// for long, skinny products).
-struct GemmTile {
-    int job, i0, j0, k0, k1;
-    long long p;
-};
-
-struct GemmRed {
-    long long p;
-    int job, slices;
-};
-
-constexpr int kGT = 64;   // output tile edge
-constexpr int kGK = 16;   // k step staged in shared memory
-
-__global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ jobs,
-                                                   const GemmTile *__restrict__ tiles, double *__restrict__ part)
-{
-    const GemmTile t = tiles[blockIdx.x];
-    const GemmJob J = jobs[t.job];
-    __shared__ double As[kGK][kGT + 1];
-    __shared__ double Bs[kGK][kGT + 1];
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
-    for (int k0 = t.k0; k0 < t.k1; k0 += kGK) {
-        for (int e = threadIdx.x; e < kGT * kGK; e += 256) {
-            // consecutive threads walk the contiguous index of the operand
-            const int i = J.ta ? e / kGK : e % kGT;
-            const int k = J.ta ? e % kGK : e / kGT;
-            const int gi = t.i0 + i, gk = k0 + k;
-            double v = 0.0;
-            if (gi < J.M && gk < t.k1) {
-                v = J.ta ? J.a[gk + (long long)gi * J.lda] : J.a[gi + (long long)gk * J.lda];
-                if (J.ks) v *= J.ks[gk];
-            }
-            As[k][i] = v;
-        }
-        for (int e = threadIdx.x; e < kGT * kGK; e += 256) {
-            const int j = J.tb ? e % kGT : e / kGK;
-            const int k = J.tb ? e / kGT : e % kGK;
-            const int gj = t.j0 + j, gk = k0 + k;
-            double v = 0.0;
-            if (gj < J.N && gk < t.k1)
-                v = J.tb ? J.b[gj + (long long)gk * J.ldb] : J.b[gk + (long long)gj * J.ldb];
-            Bs[k][j] = v;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kGK; ++k) {
-            double a[4], b[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = As[k][ty + 16 * r];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) b[c] = Bs[k][tx + 16 * c];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int i = t.i0 + ty + 16 * r, j = t.j0 + tx + 16 * c;
-            if (i < J.M && j < J.N && t.p >= 0) {
-                part[t.p + i + (long long)j * J.M] = acc[r][c];
-            } else if (i < J.M && j < J.N) {
-                double v = J.alpha * acc[r][c];
-                if (J.beta != 0.0) v = fma(J.beta, J.c[i + (long long)j * J.ldc], v);
-                J.d[i + (long long)j * J.ldd] = v;
-            }
-        }
-}
-
-// D = alpha * (sum of a split job's slices, in order) + beta C.
-__global__ void gemm_reduce_kernel(const GemmJob *__restrict__ jobs, const GemmRed *__restrict__ reds,
-                                   const double *__restrict__ part)
-{
-    const GemmRed R = reds[blockIdx.y];
-    const GemmJob J = jobs[R.job];
-    const long long mn = (long long)J.M * J.N;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < mn; e += (long long)gridDim.x * blockDim.x) {
-        double acc = 0.0;
-        for (int q = 0; q < R.slices; ++q) acc += part[R.p + q * mn + e];
-        const int i = (int)(e % J.M), j = (int)(e / J.M);
-        double v = J.alpha * acc;
-        if (J.beta != 0.0) v = fma(J.beta, J.c[i + (long long)j * J.ldc], v);
-        J.d[i + (long long)j * J.ldd] = v;
-    }
-}
 
 // One column pair of C (or one side of a term), built from its sources.
 enum ColMode { kOld = 0, kNormU = 1, kNormV = 2, kNormUV = 3 };
@@ -267,25 +161,7 @@ int launch_gemms(Arena &ar, const std::vector<GemmJob> &jobs, cudaStream_t st)
     std::vector<GemmTile> tiles;
     std::vector<GemmRed> reds;
     long long ptot = 0;
-    for (int j = 0; j < (int)jobs.size(); ++j) {
-        const GemmJob &J = jobs[j];
-        const int mt = (J.M + kGT - 1) / kGT, nt = (J.N + kGT - 1) / kGT;
-        // long, skinny products: split K into slices of >= 512
-        int slices = 1;
-        if (mt * nt <= 4 && J.K >= 1024) slices = std::min(64, J.K / 512);
-        const int chunk = ((J.K + slices - 1) / slices + kGK - 1) / kGK * kGK;
-        slices = J.K > 0 ? (J.K + chunk - 1) / chunk : 1;
-        const long long p = slices > 1 ? ptot : -1;
-        for (int q = 0; q < slices; ++q)
-            for (int i0 = 0; i0 < J.M; i0 += kGT)
-                for (int j0 = 0; j0 < J.N; j0 += kGT)
-                    tiles.push_back({j, i0, j0, q * chunk, std::min(J.K, (q + 1) * chunk),
-                                     p < 0 ? -1 : p + (long long)q * J.M * J.N});
-        if (slices > 1) {
-            reds.push_back({p, j, slices});
-            ptot += (long long)slices * J.M * J.N;
-        }
-    }
+    plan_gemm_tiles(jobs, tiles, reds, ptot);
     if (tiles.empty()) return 0;
     GemmJob *dj;
     GemmTile *dt;
@@ -294,15 +170,8 @@ int launch_gemms(Arena &ar, const std::vector<GemmJob> &jobs, cudaStream_t st)
     int rc;
     if ((rc = ar.upload(jobs, &dj)) || (rc = ar.upload(tiles, &dt))) return rc;
     if (!reds.empty() && ((rc = ar.upload(reds, &dr)) || (rc = ar.alloc(&part, ptot)))) return rc;
-    for (size_t b0 = 0; b0 < tiles.size(); b0 += 1u << 30) {
-        const unsigned nb = (unsigned)std::min<size_t>(tiles.size() - b0, 1u << 30);
-        gemm_kernel<<<nb, 256, 0, st>>>(dj, dt + b0, part);
-        note_launch();
-    }
-    if (!reds.empty()) {
-        gemm_reduce_kernel<<<dim3(16, (unsigned)reds.size()), 256, 0, st>>>(dj, dr, part);
-        note_launch();
-    }
+    run_gemm_tables(dj, dt, tiles.size(), dr, reds.size(), part, st);
+    note_launches((long long)((tiles.size() + (1u << 30) - 1) >> 30) + (reds.empty() ? 0 : 1));
     DG_CUDA(cudaGetLastError());
     return 0;
 }

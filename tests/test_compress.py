@@ -126,7 +126,7 @@ def test_gpu_compression_matches_reference_fixtures(name, a, eps):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("m,nlvl,eps", [(1024, 4, 1e-8), (512, 2, 1e-10), (768, 3, 1e-6)])
+@pytest.mark.parametrize("m,nlvl,eps", [(1024, 4, 1e-8), (512, 2, 1e-10), (768, 3, 1e-6), (2048, 3, 1e-9)])
 def test_gpu_compression_matches_restatement(m, nlvl, eps):
     api = _api()
     a = _gauss2d(m, seed=m + nlvl)
@@ -235,3 +235,15 @@ def test_python_wrapper_raises_on_invalid_arguments():
     from dplr_gb300 import _native, compress
     with pytest.raises(_native.NativeError, match="divisible"):
         compress.d2gep(np.eye(48), 1e-8, 5)
+
+
+@pytest.mark.gpu
+def test_gpu_compression_full_rank_blocks_fall_back_to_the_full_svd():
+    """Blocks of 512 with no decay (random entries): the sketch cannot pass
+    its residual check, the full SVD decides; ranks are full."""
+    api = _api()
+    a = np.random.default_rng(17).standard_normal((1024, 1024))
+    info, got = _gpu_compress(api, a, 1e-8, 1)
+    assert info == 0 and got.ne.rank == 512 and got.sw.rank == 512
+    want = gen.compress_dense(a, 1e-8, 1)
+    assert_same_tree(got, want, sig_atol=1e-12, blk_atol=1e-12)
