@@ -25,6 +25,7 @@ aggregate over ranks.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import subprocess
@@ -89,17 +90,23 @@ class ClockSampler:
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # the sampler never outlives the run, even one that raises
+            atexit.register(self._end)
         except Exception:
             self.proc = None
+
+    def _end(self):
+        if self.proc is not None and self.proc.poll() is None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
 
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
+        self._end()
         rows = []
         for line in open(self.path):
             parts = [x.strip() for x in line.split(",")]
@@ -522,25 +529,29 @@ def run_secondary(args):
     world, rank, local = dist_init()
     torch.cuda.set_device(local)
     sampler = ClockSampler(local)
-    if args.workload == "apply":
-        t, stats = build_matrix(args, device=f"cuda:{local}")
-        from dplr_gb300.plan import GpuPlan
-        plan = GpuPlan(t)
-        sampler.start()
-        out = workloads.apply_workload(plan, args.n, max(args.steps, 10), args.warmup, ROOT)
-    elif args.workload == "batched":
-        sampler.start()
-        out = workloads.batched_workload(max(args.steps, 10), args.warmup)
-    elif args.workload == "ppmm":
-        sampler.start()
-        out = workloads.ppmm_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
-    elif args.workload == "compress":
-        sampler.start()
-        out = workloads.compress_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
-    else:
-        sampler.start()
-        out = workloads.adjoint_workload(max(args.steps, 5), args.warmup)
-    out["clocks"] = sampler.stop()
+    try:
+        if args.workload == "apply":
+            t, stats = build_matrix(args, device=f"cuda:{local}")
+            from dplr_gb300.plan import GpuPlan
+            plan = GpuPlan(t)
+            sampler.start()
+            out = workloads.apply_workload(plan, args.n, max(args.steps, 10), args.warmup, ROOT)
+        elif args.workload == "batched":
+            sampler.start()
+            out = workloads.batched_workload(max(args.steps, 10), args.warmup)
+        elif args.workload == "ppmm":
+            sampler.start()
+            out = workloads.ppmm_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
+        elif args.workload == "compress":
+            sampler.start()
+            out = workloads.compress_workload(max(args.steps, 3), args.warmup,
+                                              cpu=not args.no_cpu and rank == 0)
+        else:
+            sampler.start()
+            out = workloads.adjoint_workload(max(args.steps, 5), args.warmup)
+    finally:
+        clocks = sampler.stop()
+    out["clocks"] = clocks
     out.update({"n_gpus": 1, "steps": out.pop("steps", max(args.steps, 10)), "warmup": max(3, args.warmup),
                 "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
     if rank == 0:

@@ -61,3 +61,29 @@ def test_single_process_defaults(monkeypatch):
     assert bench.dist_init() == (1, 0, 0)
     assert bench.max_over_ranks(7.5, 1, "cpu") == 7.5
     bench.barrier(1)
+
+
+def test_clock_sampler_child_never_outlives_the_run(monkeypatch):
+    """A workload that raises still stops the sampler's child process."""
+    import subprocess
+    sys.path.insert(0, ROOT)
+    import bench
+    real = subprocess.Popen
+    started = []
+
+    def fake(cmd, **kw):
+        p = real(["sleep", "30"], **kw)
+        started.append(p)
+        return p
+
+    monkeypatch.setattr(bench.subprocess, "Popen", fake)
+    s = bench.ClockSampler(0)
+    try:
+        s.start()
+        raise RuntimeError("workload failed")
+    except RuntimeError:
+        pass
+    finally:
+        out = s.stop()
+    assert started and started[0].poll() is not None
+    assert out["reasons"] == ["no samples"]
