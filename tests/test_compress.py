@@ -247,3 +247,9 @@ def test_gpu_compression_full_rank_blocks_fall_back_to_the_full_svd():
     assert info == 0 and got.ne.rank == 512 and got.sw.rank == 512
     want = gen.compress_dense(a, 1e-8, 1)
     assert_same_tree(got, want, sig_atol=1e-12, blk_atol=1e-12)
+
+
+def test_python_wrapper_checks_shape_before_any_device_call():
+    from dplr_gb300 import compress
+    with pytest.raises(ValueError):
+        compress.d2gep(np.zeros((4, 6)), 1e-8, 1)
