@@ -256,6 +256,14 @@ def run_reference(args):
     world, rank, local = dist_init()
     if rank != 0:
         return
+    if args.workload in ("compress", "ppmm"):
+        from dplr_gb300 import workloads
+        fn = workloads.compress_reference if args.workload == "compress" else workloads.ppmm_reference
+        out = fn(max(1, args.steps), max(0, args.warmup))
+        out.update({"n_gpus": 1, "warmup": max(0, args.warmup), "scaling": "weak", "vs_baseline": None,
+                    "data": "synthetic"})
+        print(json.dumps(out))
+        return
     import numpy as np  # noqa: F401
     torch_ok = True
     try:

@@ -305,41 +305,75 @@ def compress_workload(steps: int, warmup: int, m: int = 4096, nlvl: int = 4, eps
     out_bytes = 8 * _stored(t)
     sec = times[0]
     rec = {
-        "metric": f"dense->PLR compressions/s (dplrd2gep, N={m}, {nlvl} levels, eps={eps:g})",
+        "metric": _compress_metric(m, nlvl, eps),
         "value": 1.0 / sec, "unit": "compressions/s", "ms_per_step": sec * 1e3, "higher_is_better": True,
         "dtype": "f64", "gpu_launches": launches, "steps": steps,
         "e2e": {"value": 1.0 / sec, "unit": "compressions/s", "h2d_bytes_per_step": 8 * m * m,
                 "d2h_bytes_per_step": out_bytes},
-        "config": {"workload": f"2D Gaussian kernel, {m} uniform points in the unit square (width 0.05, "
-                               f"shift 1e-3), {nlvl} levels, eps {eps:g}; host A in, host tree out; "
+        "config": {"workload": _compress_workload_name(m, nlvl, eps) + "; "
                                "blocks >= 512: verified sketch (own Gaussian, FP64 GEMM and norm kernels; "
                                "cuSOLVER QR and SVD of the sketch), smaller blocks: cuSOLVER gesvd",
                    "ms_one_worker": times[1] * 1e3, "ms_default_workers": sec * 1e3,
                    "max_rank_by_level": ranks},
     }
     if cpu:
-        import scipy.linalg as sl
-        h = m // 2
-        eh = eps / 4.0                       # the threshold handed to each half
-        t0 = time.perf_counter()
-        half = _lapack_compress(a[:h, :h], eh, nlvl - 1, "gesvd")
-        t_half = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        sl.svd(a[:h, h:], full_matrices=False, lapack_driver="gesvd")
-        t_top = time.perf_counter() - t0
+        smp = _compress_cpu_sample(a, eps, nlvl)
         t0 = time.perf_counter()
         dd = _lapack_compress(a, eps, nlvl, "gesdd")
         t_dd = time.perf_counter() - t0
-        est = 2 * t_top + 2 * t_half
-        rec["cpu_baseline"] = {
-            "value": 1.0 / est, "unit": "compressions/s", "cores": os.cpu_count(), "kind": "port",
+        rec["cpu_baseline"] = {"value": 1.0 / smp["seconds"], "unit": "compressions/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": smp["sample"]}
+        rec["config"]["cpu_gesdd_s"] = t_dd
+        rec["config"]["ranks_match_gesdd"] = dd == _ranks_all(t)
+        rec["config"]["half_ranks_match"] = smp["half_ranks"] == _ranks_all(t.nw)
+    return rec
+
+
+def _compress_metric(m: int, nlvl: int, eps: float) -> str:
+    return f"dense->PLR compressions/s (dplrd2gep, N={m}, {nlvl} levels, eps={eps:g})"
+
+
+def _compress_workload_name(m: int, nlvl: int, eps: float) -> str:
+    return (f"2D Gaussian kernel, {m} uniform points in the unit square (width 0.05, shift 1e-3), "
+            f"{nlvl} levels, eps {eps:g}; host A in, host tree out")
+
+
+def _compress_cpu_sample(a: np.ndarray, eps: float, nlvl: int) -> dict:
+    """The reference's compression on the host cores (LAPACK dgesvd, the SVD
+    src/dplrd2p.c calls, scipy/OpenBLAS on all threads), timed on one
+    half-tree and one top-level block; the whole compression is two of
+    each."""
+    import scipy.linalg as sl
+    m = a.shape[0]
+    h = m // 2
+    t0 = time.perf_counter()
+    half = _lapack_compress(a[:h, :h], eps / 4.0, nlvl - 1, "gesvd")
+    t_half = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sl.svd(a[:h, h:], full_matrices=False, lapack_driver="gesvd")
+    t_top = time.perf_counter() - t0
+    return {"seconds": 2 * t_top + 2 * t_half, "half_ranks": half,
             "sample": (f"LAPACK dgesvd (the reference's SVD, scipy/OpenBLAS, all host threads): one "
                        f"half-tree ({h}, {nlvl - 1} levels) {t_half:.2f} s and one top-level block "
                        f"{t_top:.2f} s timed; whole compression = 2 x both")}
-        rec["config"]["cpu_gesdd_s"] = t_dd
-        rec["config"]["ranks_match_gesdd"] = dd == _ranks_all(t)
-        rec["config"]["half_ranks_match"] = half == _ranks_all(t.nw)
-    return rec
+
+
+def compress_reference(steps: int, warmup: int, m: int = 4096, nlvl: int = 4, eps: float = 1e-8) -> dict:
+    """The reference arm of the compression workload (host cores only)."""
+    a = np.asfortranarray(gauss2d_dense(m))
+    for _ in range(max(0, warmup)):
+        _compress_cpu_sample(a, eps, nlvl)
+    runs = [_compress_cpu_sample(a, eps, nlvl) for _ in range(max(1, steps))]
+    sec = sorted(r["seconds"] for r in runs)[len(runs) // 2]
+    return {
+        "metric": _compress_metric(m, nlvl, eps), "value": 1.0 / sec, "unit": "compressions/s",
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "dtype": "f64", "steps": len(runs),
+        "impl": "reference",
+        "cpu_baseline": {"value": 1.0 / sec, "unit": "compressions/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": runs[0]["sample"]},
+        "e2e": {"value": 1.0 / sec, "unit": "compressions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": _compress_workload_name(m, nlvl, eps), "parallelism": "host cores"},
+    }
 
 
 def _stored(t) -> int:
@@ -418,17 +452,15 @@ def ppmm_workload(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax
     h2d = 8 * (2 * tree.nnz(t) + 2 * n)          # A and C (two copies of the matrix)
     d2h = 8 * _stored(got)
     rec = {
-        "metric": f"PLR x PLR products/s (dplrgeppmm C := A A + 0.5 C, N={n}, host trees in and out)",
+        "metric": _ppmm_metric(n),
         "value": 1.0 / sec, "unit": "products/s", "ms_per_step": sec * 1e3, "higher_is_better": True,
         "dtype": "f64", "gpu_launches": launches, "steps": steps,
         "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "config": {"workload": f"2D Gaussian kernel PLR, N={n}, leaf {leaf}, ranks up to {rmax}; "
-                               f"C := A A + 0.5 C with eps {eps:g}",
+        "config": {"workload": _ppmm_workload_name(n, leaf, rmax, eps),
                    "ranks_in": tree.ranks_by_level(t), "ranks_out": tree.ranks_by_level(got),
                    "stored_doubles_in": _stored(t), "stored_doubles_out": _stored(got)},
     }
     if cpu:
-        import os
         from oracle import ppmm as oppmm
         c = copy.deepcopy(t)
         t0 = time.perf_counter()
@@ -440,3 +472,39 @@ def ppmm_workload(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax
                       f"on all host threads): {cpu_s:.2f} s"}
         rec["config"]["max_rel_diff_vs_cpu"] = _max_rel_diff(got, c)
     return rec
+
+
+def _ppmm_metric(n: int) -> str:
+    return f"PLR x PLR products/s (dplrgeppmm C := A A + 0.5 C, N={n}, host trees in and out)"
+
+
+def _ppmm_workload_name(n: int, leaf: int, rmax: int, eps: float) -> str:
+    return f"2D Gaussian kernel PLR, N={n}, leaf {leaf}, ranks up to {rmax}; C := A A + 0.5 C with eps {eps:g}"
+
+
+def ppmm_reference(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax: int = 64,
+                   eps: float = 1e-8) -> dict:
+    """The reference arm of the product workload: the restatement of
+    src/dplrppmm.c (oracle/ppmm.py, numpy BLAS on all host threads); the
+    input tree is generated on the host."""
+    import copy
+    from . import gen_gpu
+    from oracle import ppmm as oppmm
+    t = gen_gpu.kernel_tree_2d(n=n, leaf=leaf, rmax=rmax, seed=0, device="cpu")
+    secs = []
+    for i in range(max(0, warmup) + max(1, steps)):
+        c = copy.deepcopy(t)
+        t0 = time.perf_counter()
+        oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, eps)
+        if i >= max(0, warmup):
+            secs.append(time.perf_counter() - t0)
+    sec = sorted(secs)[len(secs) // 2]
+    return {
+        "metric": _ppmm_metric(n), "value": 1.0 / sec, "unit": "products/s", "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "dtype": "f64", "steps": len(secs), "impl": "reference",
+        "cpu_baseline": {"value": 1.0 / sec, "unit": "products/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "whole products by the restatement of src/dplrppmm.c (oracle/ppmm.py, "
+                                   "numpy BLAS on all host threads), median of the timed steps"},
+        "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": _ppmm_workload_name(n, leaf, rmax, eps), "parallelism": "host cores"},
+    }

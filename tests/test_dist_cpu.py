@@ -87,3 +87,26 @@ def test_clock_sampler_child_never_outlives_the_run(monkeypatch):
         out = s.stop()
     assert started and started[0].poll() is not None
     assert out["reasons"] == ["no samples"]
+
+
+@pytest.mark.parametrize("workload,fn", [("ppmm", "ppmm_reference"), ("compress", "compress_reference")])
+def test_reference_arm_follows_the_workload(monkeypatch, capsys, workload, fn):
+    """--impl reference with a secondary workload prints that workload's
+    line (host cores only), marked impl=reference."""
+    for k in ("RANK", "LOCAL_RANK", "WORLD_SIZE"):
+        monkeypatch.delenv(k, raising=False)
+    sys.path.insert(0, ROOT)
+    import bench
+    from dplr_gb300 import workloads
+    seen = {}
+
+    def stub(steps, warmup):
+        seen["args"] = (steps, warmup)
+        return {"metric": workload, "value": 1.0, "unit": "x/s", "impl": "reference"}
+
+    monkeypatch.setattr(workloads, fn, stub)
+    args = type("A", (), {"steps": 2, "warmup": 1, "workload": workload})()
+    bench.run_reference(args)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert seen["args"] == (2, 1)
+    assert line["impl"] == "reference" and line["metric"] == workload and line["warmup"] == 1
