@@ -56,7 +56,9 @@ __global__ void __launch_bounds__(256) gemm_kernel(const GemmJob *__restrict__ j
     for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
-    for (int k0 = t.k0; k0 < t.k1; k0 += kGK) {
+    // alpha == 0: op(A) op(B) is not read (BLAS semantics, NaN-safe)
+    const int kend = J.alpha == 0.0 ? t.k0 : t.k1;
+    for (int k0 = t.k0; k0 < kend; k0 += kGK) {
         for (int e = threadIdx.x; e < kGT * kGK; e += 256) {
             // consecutive threads walk the contiguous index of the operand
             const int i = J.ta ? e / kGK : e % kGT;

@@ -203,8 +203,9 @@ def geprk(alpha: float, u: np.ndarray, s: np.ndarray, v: np.ndarray, A, eps: flo
 
 def _ppmm(alpha: float, A: _Op, B: _Op, beta: float, C, eps: float) -> None:
     if isinstance(C, Dense):
-        prod = A.dense() @ B.dense()
-        C.d = alpha * prod + (beta * C.d if beta != 0.0 else 0.0)
+        # dgemm: alpha == 0 reads neither A nor B, beta == 0 does not read C
+        prod = alpha * (A.dense() @ B.dense()) if alpha != 0.0 else np.zeros_like(C.d)
+        C.d = prod + (beta * C.d if beta != 0.0 else 0.0)
         return
     eps2 = eps / 4.0
     plmm(alpha, A.nw(), B.ne(), beta, C.ne, eps2)

@@ -171,3 +171,34 @@ def test_gpu_rejects_mismatched_structures_and_leaves_c_untouched():
     finally:
         for p in (ca, cb, cc):
             tree.free_c(p)
+
+
+def _with_nan_leaf(t):
+    """Copy of t with NaN in its first leaf."""
+    m, d = tree.flatten(t)
+    out = tree.unflatten(m, d.copy())
+    node = out
+    while isinstance(node, tree.HNode):
+        node = node.nw
+    node.d[0, 0] = np.nan
+    return out
+
+
+def test_oracle_alpha_zero_does_not_read_a_or_b():
+    a = _with_nan_leaf(gen.random_tree(128, 16, 3, seed=61))
+    b = gen.random_tree(128, 16, 2, seed=62)
+    c = gen.random_tree(128, 16, 2, seed=63)
+    dc = tree.to_dense(c)
+    oppmm.geppmm("N", "N", 0.0, a, b, 0.5, c, 1e-8)
+    np.testing.assert_allclose(tree.to_dense(c), 0.5 * dc, rtol=1e-14, atol=0)
+
+
+@pytest.mark.gpu
+def test_gpu_alpha_zero_does_not_read_a_or_b():
+    a = _with_nan_leaf(gen.random_tree(256, 32, 3, seed=61))
+    b = gen.random_tree(256, 32, 2, seed=62)
+    c = gen.random_tree(256, 32, [2, 0, 1], seed=63, capacity_extra=1)
+    got = _gpu_ppmm("T", "N", 0.0, a, b, -0.5, c, 1e-8)
+    oppmm.geppmm("T", "N", 0.0, a, b, -0.5, c, 1e-8)
+    assert np.isfinite(tree.to_dense(got)).all()
+    assert_trees_match(got, c, rtol=1e-14)
