@@ -52,6 +52,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("dplr_gpu_prepare_pairs", c_int, [c_void_p, c_void_p])
     sig("dplr_gpu_geppmm", c_int, [c_char, c_char, c_int, c_double, PDPlrMtx, PDPlrMtx, c_double,
                                    PDPlrMtx, c_double, c_void_p])
+    sig("dplr_gpu_reduce_svd", c_int, [c_int, PDPlrMtx, c_double, c_int])
     sig("dplr_gpu_d2gep", c_int, [c_int, c_void_p, c_int, PDPlrMtx, c_double, c_int, c_int,
                                   POINTER(c_int)])
     sig("dplr_gpu_scal", c_int, [c_void_p, c_double, c_void_p])

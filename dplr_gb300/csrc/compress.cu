@@ -42,6 +42,7 @@ namespace dg {
 int fail(int code, const char *fmt, ...);
 void note_launch();
 void note_launches(long long k);
+int validate_tree(int m, const DPlrMtx *A, const char *fn);
 }
 using dg::GemmJob;
 using dg::GemmRed;
@@ -390,6 +391,178 @@ struct Worker {
 
 const char *block_name(const Job &jb) { return jb.r0 < jb.c0 ? "NE" : "SW"; }
 
+// ------------------------------------------------ SVD-based recompression
+
+// R (k x r, ld k) = the upper triangle of the first k rows of a geqrf result
+// (ld lda), zeros below the diagonal.
+__global__ void triu_kernel(const double *__restrict__ a, int lda, int k, int r, double *__restrict__ R)
+{
+    const long long cnt = (long long)k * r;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % k), j = (int)(e / k);
+        R[e] = i <= j ? a[i + (long long)j * lda] : 0.0;
+    }
+}
+
+// u := u diag(s): column j of an n x r block scaled by s[j].
+__global__ void scale_cols_kernel(double *__restrict__ u, const double *__restrict__ s, int n, int r)
+{
+    const long long cnt = (long long)n * r;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (long long)gridDim.x * blockDim.x)
+        u[e] *= s[e / n];
+}
+
+// One low-rank block to recompress: its host node and threshold.
+struct RJob {
+    DPlrMtx *L;
+    double eps;
+};
+
+// Buffers of one recompression worker, sized for the largest block.
+struct RWorker {
+    cudaStream_t st = nullptr;
+    cusolverDnHandle_t h = nullptr;
+    double *U = nullptr, *V = nullptr, *Ru = nullptr, *Rv = nullptr, *M = nullptr, *Um = nullptr, *Vmt = nullptr,
+           *S = nullptr, *sg = nullptr, *tau = nullptr, *work = nullptr, *rwork = nullptr, *Un = nullptr,
+           *Vn = nullptr;
+    int *info = nullptr;
+    int lwork = 0;
+    std::vector<double> hS;
+
+    bool init(int nmax, int rmax)
+    {
+        const int kmax = std::max(1, std::min(nmax, rmax));
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (solver().create(&h) != CUSOLVER_STATUS_SUCCESS || solver().set_stream(h, st) != CUSOLVER_STATUS_SUCCESS)
+            return false;
+        int a = 0, b = 0, c = 0;
+        if (solver().geqrf_size(h, nmax, rmax, U, nmax, &a) != CUSOLVER_STATUS_SUCCESS ||
+            solver().orgqr_size(h, nmax, kmax, kmax, U, nmax, S, &b) != CUSOLVER_STATUS_SUCCESS ||
+            solver().gesvd_size(h, kmax, kmax, &c) != CUSOLVER_STATUS_SUCCESS)
+            return false;
+        lwork = std::max({a, b, c, 1});
+        const size_t nr = (size_t)nmax * rmax, kr = (size_t)kmax * rmax, kk = (size_t)kmax * kmax,
+                     nk = (size_t)nmax * kmax;
+        bool ok = true;
+        for (auto pr : {std::make_pair(&U, nr), std::make_pair(&V, nr), std::make_pair(&Ru, kr), std::make_pair(&Rv, kr),
+                        std::make_pair(&M, kk), std::make_pair(&Um, kk), std::make_pair(&Vmt, kk),
+                        std::make_pair(&S, (size_t)kmax), std::make_pair(&sg, (size_t)rmax),
+                        std::make_pair(&tau, (size_t)kmax),
+                        std::make_pair(&work, (size_t)lwork), std::make_pair(&rwork, (size_t)kmax),
+                        std::make_pair(&Un, nk), std::make_pair(&Vn, nk)})
+            ok = ok && cudaMalloc((void **)pr.first, std::max<size_t>(pr.second, 1) * sizeof(double)) == cudaSuccess;
+        return ok && cudaMalloc((void **)&info, sizeof(int)) == cudaSuccess;
+    }
+
+    void release()
+    {
+        for (double *q : {U, V, Ru, Rv, M, Um, Vmt, S, sg, tau, work, rwork, Un, Vn}) cudaFree(q);
+        cudaFree(info);
+        if (h) solver().destroy(h);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    bool gemm(const GemmJob &J)
+    {
+        std::vector<GemmJob> jobs{J};
+        std::vector<GemmTile> tiles;
+        std::vector<GemmRed> reds;
+        long long ptot = 0;
+        plan_gemm_tiles(jobs, tiles, reds, ptot);
+        if (tiles.empty()) return true;
+        GemmJob *dj = nullptr;
+        GemmTile *dt = nullptr;
+        GemmRed *dr = nullptr;
+        double *part = nullptr;
+        bool ok = cudaMallocAsync((void **)&dj, sizeof(GemmJob), st) == cudaSuccess &&
+                  cudaMallocAsync((void **)&dt, sizeof(GemmTile) * tiles.size(), st) == cudaSuccess &&
+                  cudaMemcpyAsync(dj, jobs.data(), sizeof(GemmJob), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+                  cudaMemcpyAsync(dt, tiles.data(), sizeof(GemmTile) * tiles.size(), cudaMemcpyHostToDevice, st) ==
+                      cudaSuccess;
+        if (ok && !reds.empty())
+            ok = cudaMallocAsync((void **)&dr, sizeof(GemmRed) * reds.size(), st) == cudaSuccess &&
+                 cudaMallocAsync((void **)&part, sizeof(double) * ptot, st) == cudaSuccess &&
+                 cudaMemcpyAsync(dr, reds.data(), sizeof(GemmRed) * reds.size(), cudaMemcpyHostToDevice, st) ==
+                     cudaSuccess;
+        if (ok) {
+            run_gemm_tables(dj, dt, tiles.size(), dr, reds.size(), part, st);
+            dg::note_launches((long long)((tiles.size() + (1u << 30) - 1) >> 30) + (reds.empty() ? 0 : 1));
+            ok = cudaGetLastError() == cudaSuccess;
+        }
+        for (void *q : {(void *)dj, (void *)dt, (void *)dr, (void *)part})
+            if (q) cudaFreeAsync(q, st);
+        return ok;
+    }
+
+    // U diag(s) V^T (n x n, rank r) -> its SVD truncated where sigma < eps:
+    // QR of U diag(s) and of V, SVD of Ru Rv^T (k x k, k = min(n, r)).
+    // 0 done, 1 the SVD did not converge (block left as it was), -1 error.
+    int run(RJob &jb)
+    {
+        DPlrMtx *L = jb.L;
+        const int n = L->size, r = L->dlr.rank;
+        if (r == 0 || n == 0) return 0;
+        const int k = std::min(n, r);
+        const size_t nr = (size_t)n * r;
+        if (cudaMemcpyAsync(U, L->dlr.u, nr * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(V, L->dlr.v, nr * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(sg, L->dlr.sig, (size_t)r * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return -1;
+        scale_cols_kernel<<<128, 256, 0, st>>>(U, sg, n, r);
+        dg::note_launch();
+        if (solver().geqrf(h, n, r, U, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS) return -1;
+        triu_kernel<<<64, 256, 0, st>>>(U, n, k, r, Ru);
+        dg::note_launch();
+        if (solver().orgqr(h, n, k, k, U, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS) return -1;
+        if (solver().geqrf(h, n, r, V, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS) return -1;
+        triu_kernel<<<64, 256, 0, st>>>(V, n, k, r, Rv);
+        dg::note_launch();
+        if (solver().orgqr(h, n, k, k, V, n, tau, work, lwork, info) != CUSOLVER_STATUS_SUCCESS) return -1;
+        if (cudaGetLastError() != cudaSuccess) return -1;
+        // M = Ru Rv^T (k x k)
+        if (!gemm({Ru, Rv, nullptr, nullptr, M, k, k, r, k, k, 0, k, 0, 1, 1.0, 0.0})) return -1;
+        if (solver().gesvd(h, 'S', 'S', k, k, M, k, S, Um, k, Vmt, k, work, lwork, rwork, info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return -1;
+        int devinfo = 0;
+        hS.resize(k);
+        if (cudaMemcpyAsync(&devinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(hS.data(), S, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return -1;
+        if (devinfo != 0) return 1;
+        int rank = 0;
+        while (rank < k && !(hS[rank] < jb.eps)) ++rank;
+        if (rank > 0) {
+            // U_new = Qu Um[:, :rank], V_new = Qv Vm[:, :rank] = Qv (Vm^T)^T
+            if (!gemm({U, Um, nullptr, nullptr, Un, n, rank, k, n, k, 0, n, 0, 0, 1.0, 0.0}) ||
+                !gemm({V, Vmt, nullptr, nullptr, Vn, n, rank, k, n, k, 0, n, 0, 1, 1.0, 0.0}))
+                return -1;
+            if (cudaMemcpyAsync(L->dlr.u, Un, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaMemcpyAsync(L->dlr.v, Vn, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return -1;
+            memcpy(L->dlr.sig, hS.data(), (size_t)rank * sizeof(double));
+        }
+        L->dlr.rank = rank;
+        return 0;
+    }
+};
+
+void collect_rjobs(DPlrMtx *A, double eps, std::vector<RJob> &jobs)
+{
+    if (A->type != PLR_HMTX) return;
+    const double e2 = eps / 4.0;
+    jobs.push_back({A->dh.ne, e2});
+    jobs.push_back({A->dh.sw, e2});
+    collect_rjobs(A->dh.nw, e2, jobs);
+    collect_rjobs(A->dh.se, e2, jobs);
+}
+
 }  // namespace
 
 extern "C" {
@@ -489,6 +662,52 @@ int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int 
     }
     *info = 0;
     return DPLR_GPU_OK;
+}
+
+int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers)
+{
+    const char *fn = "dplr_gpu_reduce_svd";
+    if (m < 0) return dg::fail(DPLR_GPU_EINVAL, "%s: invalid matrix size %d", fn, m);
+    if (!A) return dg::fail(DPLR_GPU_EINVAL, "%s: null argument", fn);
+    if (!(eps >= 0.0)) return dg::fail(DPLR_GPU_EINVAL, "%s: eps must be nonnegative", fn);
+    int rc = dg::validate_tree(m, A, fn);
+    if (rc) return rc;
+    std::vector<RJob> jobs;
+    collect_rjobs(A, eps, jobs);
+    int nmax = 0, rmax = 0;
+    for (const RJob &j : jobs)
+        if (j.L->dlr.rank > 0) {
+            nmax = std::max(nmax, j.L->size);
+            rmax = std::max(rmax, j.L->dlr.rank);
+        }
+    if (rmax == 0) return 0;
+    if (!solver().ok) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: cannot load cuSOLVER (libcusolver.so.12)");
+    std::stable_sort(jobs.begin(), jobs.end(), [](const RJob &a, const RJob &b) {
+        return (long long)a.L->size * a.L->dlr.rank > (long long)b.L->size * b.L->dlr.rank;
+    });
+    int nw = workers > 0 ? workers : 8;
+    nw = std::max(1, std::min<int>(nw, (int)jobs.size()));
+    std::vector<RWorker> pool(nw);
+    bool ok = true;
+    for (RWorker &w : pool) ok = ok && w.init(nmax, rmax);
+    std::vector<int> res(jobs.size(), 0);
+    if (ok) {
+        std::atomic<int> next{0};
+        auto body = [&](RWorker &w) {
+            for (int k = next.fetch_add(1); k < (int)jobs.size(); k = next.fetch_add(1)) res[k] = w.run(jobs[k]);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nw; ++t) th.emplace_back(body, std::ref(pool[t]));
+        body(pool[0]);
+        for (std::thread &t : th) t.join();
+    }
+    for (RWorker &w : pool) w.release();
+    if (!ok) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: device setup failed");
+    for (int r : res) {
+        if (r < 0) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: CUDA or cuSOLVER call failed");
+        if (r > 0) return report(DPLR_GPU_ENOTCONV, "dplr_gpu_reduce_svd: an SVD did not converge (block kept)");
+    }
+    return 0;
 }
 
 void dplrd2gep(int m, double *A, int lda, DPlrMtx *B, double eps, int nlvl, int *info)

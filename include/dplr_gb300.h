@@ -247,6 +247,15 @@ DPLR_API int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlr
  * (at 1.5x the largest result so far) for later calls; this frees it. */
 DPLR_API void dplr_gpu_release_staging(void);
 
+/* SVD-based recompression of every low-rank block of a host tree, the
+ * alternative to dplrreduce's Gram-Schmidt (dortlr): each U diag(s) V^T
+ * becomes its truncated SVD (QR of U diag(s) and of V, SVD of Ru Rv^T on
+ * the GPU), keeping the singular values >= the block's threshold, eps/4
+ * per level as dplrreduce splits it.  Ranks only shrink, capacities stay.
+ * workers: host threads with their own stream and cuSOLVER handle (0 = 8).
+ * DPLR_GPU_ENOTCONV if an SVD did not converge (that block is kept). */
+DPLR_API int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers);
+
 /* Associate the drop-in entry points with a plan for this host tree
  * (they then skip the upload).  dplr_gpu_unregister drops the link. */
 DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);

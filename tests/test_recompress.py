@@ -1,0 +1,137 @@
+"""SVD-based recompression (dplr_gpu_reduce_svd), the alternative to
+dplrreduce's Gram-Schmidt with dplrreduce's thresholds (eps/4 per level,
+src/dplrreduce.c:46).
+
+The restatement (oracle/recompress.py) is pinned on the CPU to the
+definition: every block becomes its exact SVD truncated below the block's
+threshold.  The GPU is held to the restatement: equal ranks and
+capacities, singular values and blocks to rounding.
+"""
+import numpy as np
+import pytest
+
+from dplr_gb300 import gen, tree
+from oracle import recompress as orec
+
+
+def _doubled(t):
+    """t with every low-rank block written twice side by side: the same
+    matrix times 2 at twice the rank (what an append without
+    recompression produces)."""
+    if isinstance(t, tree.HNode):
+        def dup(L):
+            return tree.LowRank(np.hstack([L.u, L.u]), np.concatenate([L.sig, L.sig]),
+                                np.hstack([L.v, L.v]), capacity=2 * L.rank + 3)
+        return tree.HNode(_doubled(t.nw), dup(t.ne), _doubled(t.se), dup(t.sw))
+    return tree.Dense(2.0 * t.d)
+
+
+def _blocks(t, out=None, eps=None, e=None):
+    """[(block, threshold)] in pre-order, thresholds eps/4 per level."""
+    out = [] if out is None else out
+    if isinstance(t, tree.HNode):
+        e2 = (eps if e is None else e) / 4.0
+        out += [(t.ne, e2), (t.sw, e2)]
+        _blocks(t.nw, out, eps, e2)
+        _blocks(t.se, out, eps, e2)
+    return out
+
+
+def assert_same_blocks(got, want, tol):
+    for (g, _), (w, _) in zip(_blocks(got, eps=1.0), _blocks(want, eps=1.0)):
+        assert g.rank == w.rank and g.capacity == w.capacity
+        if w.rank:
+            scale = max(1.0, float(w.sig[0]))
+            np.testing.assert_allclose(g.sig, w.sig, rtol=0, atol=tol * scale)
+            np.testing.assert_allclose((g.u * g.sig) @ g.v.T, (w.u * w.sig) @ w.v.T, rtol=0, atol=tol * scale)
+
+
+# ---------------------------------------------------------------- CPU -----
+
+def test_restatement_is_the_truncated_svd_of_every_block():
+    t = _doubled(gen.random_tree(256, 32, [7, 5, 3], seed=3, diag_shift=2.0))
+    eps = 1e-6
+    r = orec.reduce_svd(t, eps)
+    for (L, thr), (R, _) in zip(_blocks(t, eps=eps), _blocks(r, eps=eps)):
+        s = np.linalg.svd((L.u * L.sig) @ L.v.T, compute_uv=False)
+        keep = s[s >= thr]
+        assert R.rank == len(keep) == L.rank // 2          # the doubled columns collapse
+        np.testing.assert_allclose(R.sig, keep, rtol=1e-12)
+        assert R.capacity == L.capacity
+    np.testing.assert_allclose(tree.to_dense(r), tree.to_dense(t), atol=1e-12)
+
+
+def test_restatement_drops_columns_below_the_threshold():
+    t = gen.random_tree(256, 32, 8, seed=4, decay=0.1)    # sig decays by 10x per column
+    r = orec.reduce_svd(t, 1e-2)
+    assert max(tree.ranks_by_level(r)) < max(tree.ranks_by_level(t))
+    err = np.abs(tree.to_dense(r) - tree.to_dense(t)).max()
+    assert err <= 1e-2
+
+
+# ---------------------------------------------------------------- GPU -----
+
+def _gpu(t, eps, workers=0):
+    from dplr_gb300 import compress
+    return compress.reduce_svd(t, eps, workers)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eps", [1e-9, 1e-4, 1e-1])
+def test_gpu_matches_restatement(eps):
+    t = _doubled(gen.random_tree(1024, 64, [9, 7, 5, 3], seed=5, diag_shift=2.0, decay=0.3))
+    got = _gpu(t, eps)
+    assert_same_blocks(got, orec.reduce_svd(t, eps), tol=1e-12)
+    for g, w in zip([g for g, _ in _blocks(got, eps=1.0)], [w for w, _ in _blocks(t, eps=1.0)]):
+        assert g.rank <= w.rank
+
+
+@pytest.mark.gpu
+def test_gpu_handles_rank_above_block_size():
+    """Blocks of 16 rows carrying 40 columns (as products and appends leave
+    them): k = min(n, r) = 16 singular values at most."""
+    rng = np.random.default_rng(8)
+
+    def lr(n, r):
+        return tree.LowRank(rng.standard_normal((n, r)), np.abs(rng.standard_normal(r)) + 0.1,
+                            rng.standard_normal((n, r)), capacity=r + 2)
+
+    t = tree.HNode(tree.Dense(rng.standard_normal((16, 16))), lr(16, 40),
+                   tree.Dense(rng.standard_normal((16, 16))), lr(16, 40))
+    got = _gpu(t, 1e-10)
+    assert got.ne.rank == 16 and got.sw.rank == 16
+    assert_same_blocks(got, orec.reduce_svd(t, 1e-10), tol=1e-11)
+    np.testing.assert_allclose(tree.to_dense(got), tree.to_dense(t), atol=1e-10)
+
+
+@pytest.mark.gpu
+def test_gpu_bounds_the_rank_growth_of_a_product():
+    """C = A A of a compressed kernel grows ranks by appending; the SVD
+    recompression brings them back down within the threshold."""
+    from dplr_gb300 import _native, workloads
+    a = gen.compress_dense(workloads.gauss2d_dense(512, seed=2), 1e-10, 3)
+    api = _native.api()
+    ca, cc = tree.to_c(a), tree.to_c(a)
+    try:
+        api.geppmm("N", "N", 512, 1.0, ca, ca, 0.0, cc, 1e-12)
+        c = tree.from_c(cc)
+    finally:
+        tree.free_c(ca)
+        tree.free_c(cc)
+    r = _gpu(c, 1e-8, workers=3)
+    assert max(tree.ranks_by_level(r)) < max(tree.ranks_by_level(c))
+    assert np.abs(tree.to_dense(r) - tree.to_dense(c)).max() <= 1e-8 * 3
+    assert_same_blocks(r, orec.reduce_svd(c, 1e-8), tol=1e-11)
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_invalid_arguments():
+    from dplr_gb300 import _native
+    lib = _native.lib()
+    c = tree.to_c(gen.random_tree(64, 16, 2, seed=1))
+    try:
+        assert lib.dplr_gpu_reduce_svd(-1, c, 1e-8, 0) == -1
+        assert lib.dplr_gpu_reduce_svd(64, c, -1.0, 0) == -1
+        assert lib.dplr_gpu_reduce_svd(32, c, 1e-8, 0) == -1
+    finally:
+        tree.free_c(c)
