@@ -2,8 +2,8 @@
 //
 // FP64 FMA (DFMA), FP64 tensor MMA (mma.sync m8n8k4 f64), FP32 FMA and a
 // streaming double4 copy.  The FP64 numbers are the roofline denominators
-// of the FP64 kernels (the measured peaks cover only the copy
-// bandwidth and bf16 GEMM).  Run with:  python -m dplr_gb300.diag.peak_probe
+// of the FP64 kernels (MEASURED_PEAKS.json holds only the copy bandwidth
+// and the bf16 GEMM rate).  Run with:  python -m dplr_gb300.diag.peak_probe
 #include <cstdio>
 #include <cuda_runtime.h>
 #define CK(x) do{cudaError_t e=(x); if(e!=cudaSuccess){printf("ERR %s line %d: %s\n",#x,__LINE__,cudaGetErrorString(e)); return 1;}}while(0)
