@@ -12,7 +12,11 @@ from dplr_gb300 import gen, tree
 
 @pytest.fixture(scope="module")
 def lib():
+    import os
     from dplr_gb300 import _native
+    if not os.path.exists(_native.LIB_PATH):
+        from dplr_gb300 import build
+        build.build()
     return _native.lib()
 
 
