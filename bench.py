@@ -234,6 +234,44 @@ def cpu_sample(t, args, threads: int):
     }
 
 
+def ppmm_cpu_leg(t, got):
+    """One product C := A A + 0.5 C by the restatement of src/dplrppmm.c
+    (oracle/ppmm.py, numpy BLAS on all host threads) on the GPU leg's
+    input; returns its cpu_baseline entry and the largest difference from
+    the GPU's product."""
+    import copy
+
+    from dplr_gb300 import workloads
+    from oracle import ppmm as oppmm
+    c = copy.deepcopy(t)
+    t0 = time.perf_counter()
+    oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, workloads.PPMM["eps"])
+    sec = time.perf_counter() - t0
+    cb = {"value": 1.0 / sec, "unit": "products/s", "cores": os.cpu_count(), "kind": "port",
+          "sample": f"one whole product by the restatement of src/dplrppmm.c (oracle/ppmm.py, numpy BLAS "
+                    f"on all host threads): {sec:.2f} s"}
+    return cb, workloads._max_rel_diff(got, c)
+
+
+def ppmm_reference_arm(steps: int, warmup: int) -> dict:
+    """The reference arm of the product workload, on the host cores only:
+    the input is generated on the host, each step is one whole product by
+    the restatement of src/dplrppmm.c."""
+    import copy
+
+    from dplr_gb300 import workloads
+    from oracle import ppmm as oppmm
+    t = workloads.ppmm_input("cpu")
+    secs = []
+    for i in range(warmup + steps):
+        c = copy.deepcopy(t)
+        t0 = time.perf_counter()
+        oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, workloads.PPMM["eps"])
+        if i >= warmup:
+            secs.append(time.perf_counter() - t0)
+    return workloads.ppmm_reference_record(secs)
+
+
 def inverse_nnz(t) -> int:
     """dplrnz of DPLR's explicit inverse: every block keeps its own rank and
     gains the rank of each ancestor's correction on its side."""
@@ -258,7 +296,7 @@ def run_reference(args):
         return
     if args.workload in ("compress", "ppmm"):
         from dplr_gb300 import workloads
-        fn = workloads.compress_reference if args.workload == "compress" else workloads.ppmm_reference
+        fn = workloads.compress_reference if args.workload == "compress" else ppmm_reference_arm
         out = fn(max(1, args.steps), max(0, args.warmup))
         out.update({"n_gpus": 1, "warmup": max(0, args.warmup), "scaling": "weak", "vs_baseline": None,
                     "data": "synthetic"})
@@ -552,8 +590,13 @@ def run_secondary(args):
             sampler.start()
             out = workloads.batched_workload(max(args.steps, 10), args.warmup)
         elif args.workload == "ppmm":
+            t = workloads.ppmm_input(f"cuda:{local}")
             sampler.start()
-            out = workloads.ppmm_workload(max(args.steps, 3), args.warmup, cpu=not args.no_cpu and rank == 0)
+            out, got = workloads.ppmm_workload(t, max(args.steps, 3), args.warmup)
+            if not args.no_cpu and rank == 0:
+                cb, diff = ppmm_cpu_leg(t, got)
+                out["cpu_baseline"] = cb
+                out["config"]["max_rel_diff_vs_cpu"] = diff
         elif args.workload == "compress":
             sampler.start()
             out = workloads.compress_workload(max(args.steps, 3), args.warmup,

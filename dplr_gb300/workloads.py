@@ -28,9 +28,9 @@
 * ``ppmm``: the PLR x PLR product C := A A + 0.5 C (dplrgeppmm) on the 2D
   Gaussian-kernel matrix of the solve benchmark at N = 16384 (leaf 256,
   ranks up to 64), eps = 1e-8; one step is one host-to-host call (A and C
-  uploaded, C's grown tree copied back).  The CPU leg is the restatement
-  oracle/ppmm.py (the reference's recursion, numpy BLAS on all host
-  threads) on the same inputs; its result is the parity check.
+  uploaded, C's grown tree copied back).  bench.py adds the CPU leg (the
+  restatement of the reference's recursion on all host threads, on the
+  same inputs), whose result is also the parity check.
 
 Each returns the JSON record of its line; the caller adds clocks.
 """
@@ -420,12 +420,20 @@ def _max_rel_diff(a, b) -> float:
     return out
 
 
-def ppmm_workload(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax: int = 64,
-                  eps: float = 1e-8, cpu: bool = True) -> dict:
-    import copy
-    import ctypes
+PPMM = {"n": 16384, "leaf": 256, "rmax": 64, "eps": 1e-8}
+
+
+def ppmm_input(device: str):
+    """A of the product workload: the 2D Gaussian-kernel PLR of the solve
+    benchmark at N = 16384 (leaf 256, ranks up to 64)."""
     from . import gen_gpu
-    t = gen_gpu.kernel_tree_2d(n=n, leaf=leaf, rmax=rmax, seed=0, device="cuda")
+    return gen_gpu.kernel_tree_2d(n=PPMM["n"], leaf=PPMM["leaf"], rmax=PPMM["rmax"], seed=0, device=device)
+
+
+def ppmm_workload(t, steps: int, warmup: int):
+    """C := A A + 0.5 C (C = A) through dplr_gpu_geppmm, host trees in and
+    out; returns the record and the last product."""
+    n, eps = t.size, PPMM["eps"]
     lib = _native.lib()
     ca = tree.to_c(t)
     nw = max(3, warmup)
@@ -456,22 +464,11 @@ def ppmm_workload(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax
         "value": 1.0 / sec, "unit": "products/s", "ms_per_step": sec * 1e3, "higher_is_better": True,
         "dtype": "f64", "gpu_launches": launches, "steps": steps,
         "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "config": {"workload": _ppmm_workload_name(n, leaf, rmax, eps),
+        "config": {"workload": _ppmm_workload_name(n, PPMM["leaf"], PPMM["rmax"], eps),
                    "ranks_in": tree.ranks_by_level(t), "ranks_out": tree.ranks_by_level(got),
                    "stored_doubles_in": _stored(t), "stored_doubles_out": _stored(got)},
     }
-    if cpu:
-        from oracle import ppmm as oppmm
-        c = copy.deepcopy(t)
-        t0 = time.perf_counter()
-        oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, eps)
-        cpu_s = time.perf_counter() - t0
-        rec["cpu_baseline"] = {
-            "value": 1.0 / cpu_s, "unit": "products/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"one whole product by the restatement of src/dplrppmm.c (oracle/ppmm.py, numpy BLAS "
-                      f"on all host threads): {cpu_s:.2f} s"}
-        rec["config"]["max_rel_diff_vs_cpu"] = _max_rel_diff(got, c)
-    return rec
+    return rec, got
 
 
 def _ppmm_metric(n: int) -> str:
@@ -482,29 +479,18 @@ def _ppmm_workload_name(n: int, leaf: int, rmax: int, eps: float) -> str:
     return f"2D Gaussian kernel PLR, N={n}, leaf {leaf}, ranks up to {rmax}; C := A A + 0.5 C with eps {eps:g}"
 
 
-def ppmm_reference(steps: int, warmup: int, n: int = 16384, leaf: int = 256, rmax: int = 64,
-                   eps: float = 1e-8) -> dict:
-    """The reference arm of the product workload: the restatement of
-    src/dplrppmm.c (oracle/ppmm.py, numpy BLAS on all host threads); the
-    input tree is generated on the host."""
-    import copy
-    from . import gen_gpu
-    from oracle import ppmm as oppmm
-    t = gen_gpu.kernel_tree_2d(n=n, leaf=leaf, rmax=rmax, seed=0, device="cpu")
-    secs = []
-    for i in range(max(0, warmup) + max(1, steps)):
-        c = copy.deepcopy(t)
-        t0 = time.perf_counter()
-        oppmm.geppmm("N", "N", 1.0, t, t, 0.5, c, eps)
-        if i >= max(0, warmup):
-            secs.append(time.perf_counter() - t0)
-    sec = sorted(secs)[len(secs) // 2]
+def ppmm_reference_record(seconds: list) -> dict:
+    """The reference arm's line of the product workload from the timed
+    products (host cores)."""
+    sec = sorted(seconds)[len(seconds) // 2]
+    n = PPMM["n"]
     return {
         "metric": _ppmm_metric(n), "value": 1.0 / sec, "unit": "products/s", "ms_per_step": sec * 1e3,
-        "higher_is_better": True, "dtype": "f64", "steps": len(secs), "impl": "reference",
+        "higher_is_better": True, "dtype": "f64", "steps": len(seconds), "impl": "reference",
         "cpu_baseline": {"value": 1.0 / sec, "unit": "products/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "whole products by the restatement of src/dplrppmm.c (oracle/ppmm.py, "
-                                   "numpy BLAS on all host threads), median of the timed steps"},
+                         "sample": "whole products by the restatement of src/dplrppmm.c (numpy BLAS on all "
+                                   "host threads), median of the timed steps"},
         "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "config": {"workload": _ppmm_workload_name(n, leaf, rmax, eps), "parallelism": "host cores"},
+        "config": {"workload": _ppmm_workload_name(n, PPMM["leaf"], PPMM["rmax"], PPMM["eps"]),
+                   "parallelism": "host cores"},
     }

@@ -89,7 +89,7 @@ def test_clock_sampler_child_never_outlives_the_run(monkeypatch):
     assert out["reasons"] == ["no samples"]
 
 
-@pytest.mark.parametrize("workload,fn", [("ppmm", "ppmm_reference"), ("compress", "compress_reference")])
+@pytest.mark.parametrize("workload,fn", [("ppmm", "ppmm_reference_arm"), ("compress", "compress_reference")])
 def test_reference_arm_follows_the_workload(monkeypatch, capsys, workload, fn):
     """--impl reference with a secondary workload prints that workload's
     line (host cores only), marked impl=reference."""
@@ -104,7 +104,7 @@ def test_reference_arm_follows_the_workload(monkeypatch, capsys, workload, fn):
         seen["args"] = (steps, warmup)
         return {"metric": workload, "value": 1.0, "unit": "x/s", "impl": "reference"}
 
-    monkeypatch.setattr(workloads, fn, stub)
+    monkeypatch.setattr(bench if fn == "ppmm_reference_arm" else workloads, fn, stub)
     args = type("A", (), {"steps": 2, "warmup": 1, "workload": workload})()
     bench.run_reference(args)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])

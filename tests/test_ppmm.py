@@ -202,3 +202,17 @@ def test_gpu_alpha_zero_does_not_read_a_or_b():
     oppmm.geppmm("T", "N", 0.0, a, b, -0.5, c, 1e-8)
     assert np.isfinite(tree.to_dense(got)).all()
     assert_trees_match(got, c, rtol=1e-14)
+
+
+def test_bench_cpu_leg_times_the_restatement_and_compares():
+    """bench.py's CPU leg of the product workload: one product by the
+    restatement on the given input, and its difference from a product."""
+    import copy
+
+    import bench
+    from dplr_gb300 import workloads
+    a = gen.random_tree(256, 32, [5, 3, 2], seed=71, diag_shift=2.0)
+    want = copy.deepcopy(a)
+    oppmm.geppmm("N", "N", 1.0, a, a, 0.5, want, workloads.PPMM["eps"])
+    cb, diff = bench.ppmm_cpu_leg(a, want)
+    assert cb["kind"] == "port" and cb["value"] > 0 and diff == 0.0
