@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -28,10 +29,19 @@ using namespace dg;
 
 namespace {
 
+// Registered plans are shared: a drop-in call holds its own reference for
+// the whole call, so dplr_gpu_register / dplr_gpu_unregister on the same
+// tree from another thread never frees a plan that is still in use (the
+// plan goes when its last user lets go).
 std::mutex g_reg_mu;
-std::map<const DPlrMtx *, Plan *> g_registered;
+std::map<const DPlrMtx *, std::shared_ptr<Plan>> g_registered;
 
-Plan *lookup_registered(const DPlrMtx *A, int m)
+std::shared_ptr<Plan> shared_plan(Plan *p)
+{
+    return std::shared_ptr<Plan>(p, [](Plan *q) { plan_free(q); });
+}
+
+std::shared_ptr<Plan> lookup_registered(const DPlrMtx *A, int m)
 {
     std::lock_guard<std::mutex> lk(g_reg_mu);
     auto it = g_registered.find(A);
@@ -47,6 +57,7 @@ void report(const char *fn)
 // Plan for a drop-in call: the registered one, or a temporary upload.
 struct CallPlan {
     Plan *p = nullptr;
+    std::shared_ptr<Plan> keep;
     bool owned = false;
     ~CallPlan()
     {
@@ -54,8 +65,11 @@ struct CallPlan {
     }
     int get(int m, const DPlrMtx *A)
     {
-        p = lookup_registered(A, m);
-        if (p) return 0;
+        keep = lookup_registered(A, m);
+        if (keep) {
+            p = keep.get();
+            return 0;
+        }
         owned = true;
         return plan_build(m, A, 0, &p);
     }
@@ -162,20 +176,26 @@ int dplr_gpu_register(int m, DPlrMtx *A)
     Plan *p = nullptr;
     int rc = plan_build(m, A, 0, &p);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lk(g_reg_mu);
-    auto it = g_registered.find(A);
-    if (it != g_registered.end()) plan_free(it->second);
-    g_registered[A] = p;
-    return 0;
+    std::shared_ptr<Plan> fresh = shared_plan(p), old;
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mu);
+        old.swap(g_registered[A]);
+        g_registered[A] = fresh;
+    }
+    return 0;       // `old` is released here, or by the last call still using it
 }
 
 int dplr_gpu_unregister(DPlrMtx *A)
 {
-    std::lock_guard<std::mutex> lk(g_reg_mu);
-    auto it = g_registered.find(A);
-    if (it == g_registered.end()) return fail(DPLR_GPU_EINVAL, "dplr_gpu_unregister: not registered");
-    plan_free(it->second);
-    g_registered.erase(it);
+    std::shared_ptr<Plan> old;
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mu);
+        auto it = g_registered.find(A);
+        if (it == g_registered.end())
+            return fail(DPLR_GPU_EINVAL, "dplr_gpu_unregister: not registered");
+        old.swap(it->second);
+        g_registered.erase(it);
+    }
     return 0;
 }
 

@@ -59,11 +59,40 @@ def _peaks(root):
         return 6800.0, "of fallback"
 
 
+_FP64_PEAK: dict = {}
+
+
+def fp64_gemm_peak() -> dict:
+    """FP64 roofline denominator measured in this process: cuBLAS DGEMM
+    (torch.matmul, float64, 4096^3, 2 n^3 flops), best of 5 after one warm-up,
+    timed with CUDA events.  Measured once per process."""
+    if _FP64_PEAK:
+        return _FP64_PEAK
+    n = 4096
+    g = torch.Generator(device="cuda").manual_seed(1)
+    a = torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")
+    c = torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = _events()
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    _FP64_PEAK.update({"tflops": 2.0 * n ** 3 / (best / 1e3) / 1e12,
+                       "source": "measured cuBLAS DGEMM 4096^3 in this run (best of 5)"})
+    del a, b, c
+    return _FP64_PEAK
+
+
 def apply_workload(plan: GpuPlan, n: int, steps: int, warmup: int, root: str) -> dict:
     """FP64 apply bandwidth for 1, 16 and 256 right-hand sides; the record's
     value is the 1-RHS case."""
     stream = torch.cuda.current_stream()
     hbm, src = _peaks(root)
+    fp64 = fp64_gemm_peak()["tflops"]
     rows = {}
     for nrhs in (1, 16, 256):
         tune = plan.autotune(nrhs)             # launch shapes for this right-hand-side count
@@ -83,7 +112,7 @@ def apply_workload(plan: GpuPlan, n: int, steps: int, warmup: int, root: str) ->
         by = 8.0 * plan.nnz + 16.0 * n * nrhs
         fl = 2.0 * plan.nnz * nrhs
         rows[nrhs] = {"ms": ms, "gbs": by / (ms / 1e3) / 1e9, "tflops": fl / (ms / 1e3) / 1e12,
-                      "frac_hbm": by / (ms / 1e3) / 1e9 / hbm, "frac_fp64": fl / (ms / 1e3) / 1e12 / 1.19,
+                      "frac_hbm": by / (ms / 1e3) / 1e9 / hbm, "frac_fp64": fl / (ms / 1e3) / 1e12 / fp64,
                       "autotune": tune}
     one = rows[1]
     # FP64-accurate 1-RHS apply on the FP32 pipes (float-pair copy of the
@@ -123,11 +152,12 @@ def apply_workload(plan: GpuPlan, n: int, steps: int, warmup: int, root: str) ->
                      "achieved": pgbs, "peak": hbm, "unit": "GB/s", "frac": pgbs / hbm, "traffic": None,
                      "peak_source": src,
                      "note": "FP32-pair products (exact high part) with compensated sums; the FP64 kernels "
-                             "are capped by FP64 FMA issue (1.19 TFLOP/s) at 4.76 TB/s = 70% of the copy rate"},
+                             "are capped by FP64 issue (fp64_1rhs.fp64_bound_gbs)"},
         "pairs_1rhs": pairs,
         "fp64_by_rhs": rows,
         "fp64_1rhs": {"gbs": one["gbs"], "frac_hbm": one["frac_hbm"],
-                      "fp64_bound_gbs": 1.19e12 / 2.0 * 8.0 / 1e9},
+                      "fp64_bound_gbs": fp64 * 1e12 / 2.0 * 8.0 / 1e9,
+                      "fp64_peak_tflops": fp64, "fp64_peak_source": fp64_gemm_peak()["source"]},
         "config": {"workload": f"apply of the 2D Gaussian-kernel PLR, N={n}, nnz={plan.nnz}",
                    "bytes_per_rhs": "8*nnz + 16*N (factors read once, x read and y written once)"},
     }
@@ -493,4 +523,115 @@ def ppmm_reference_record(seconds: list) -> dict:
         "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "config": {"workload": _ppmm_workload_name(n, PPMM["leaf"], PPMM["rmax"], PPMM["eps"]),
                    "parallelism": "host cores"},
+    }
+
+
+# --------------------------------------------------------------------------
+# C2: plain FP64 multi-RHS products at scale
+# --------------------------------------------------------------------------
+
+C2 = {"n": 131072, "leaf": 256, "rank": 32, "ell": 0.05, "shift": 1e-2, "rhs": 64, "seed": 0}
+
+
+def c2_input():
+    """The fixed-rank 1D exponential-kernel PLR: N = 131072 sorted uniform
+    points on [0, 1], exp(-|x_i - x_j| / 0.05) + 1e-2 I, leaf 256 (9
+    levels).  Every off-diagonal block of this kernel is exactly rank one
+    (it is semiseparable), so a rank-32 truncated SVD of it is the exact
+    rank-one factor plus 31 orthonormal tail columns with round-off-level
+    singular values; gen.exp1d_tree builds that without the dense matrix.
+    dplrnz = 2 N sum(r) + N b = 109,051,904 stored doubles (872 MB)."""
+    x = np.sort(np.random.default_rng(C2["seed"]).uniform(0.0, 1.0, C2["n"]))
+    return gen.exp1d_tree(x, ell=C2["ell"], shift=C2["shift"], leaf=C2["leaf"], rank=C2["rank"],
+                          seed=C2["seed"] + 1)
+
+
+def c2_rhs(device: str = "cuda") -> torch.Tensor:
+    g = torch.Generator(device="cpu").manual_seed(C2["seed"] + 2)
+    return torch.randn(C2["rhs"], C2["n"], generator=g, dtype=torch.float64).to(device)
+
+
+def _timed(fn, steps: int, warmup: int):
+    """Mean device milliseconds of fn() over `steps` calls after warm-up,
+    CUDA events on the current stream; factors (> L2) are re-read every call."""
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, warmup)):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def c2_workload(t, steps: int, warmup: int, root: str) -> dict:
+    """dplrgepdmm (Y = A X, 64 RHS) and the inverse apply on the C2 matrix.
+
+    The record's value is the product (RHS/s); the inverse apply is reported
+    twice: DPLR's way (the explicit inverse B = inv(A) made by the drop-in
+    dplrgeinv, then B X) and this library's Woodbury solve refined to 1e-12.
+    """
+    n, nrhs = t.size, C2["rhs"]
+    X = c2_rhs()
+    plan = GpuPlan(t)
+    Y = torch.empty_like(X)
+    l0 = _native.launch_count()
+    ms_apply = _timed(lambda: plan.apply(X, out=Y), steps, warmup)
+    launches = (_native.launch_count() - l0) // (steps + max(3, warmup))
+    flops = 2.0 * plan.nnz * nrhs
+    fp64 = fp64_gemm_peak()
+    tflops = flops / (ms_apply / 1e3) / 1e12
+    # explicit inverse (DPLR's dplrgeinv, on the GPU through the drop-in) and its apply
+    a = tree.to_c(t)
+    b_inv = tree.new_empty()
+    t0 = time.perf_counter()
+    info = _native.api().geinv(n, a, b_inv, 0.0)
+    t_inv = time.perf_counter() - t0
+    if info != 0:
+        raise RuntimeError(f"dplrgeinv failed: info {info}")
+    nnz_inv = _native.api().nz(n, b_inv)
+    pinv = GpuPlan(b_inv)
+    tree.free_c(b_inv)
+    tree.free_c(a)
+    Z = torch.empty_like(X)
+    ms_inv = _timed(lambda: pinv.apply(X, out=Z), steps, warmup)
+    res_inv = plan.residual(Z, X, precise=False)
+    rel_inv = float((res_inv.norm(dim=1) / X.norm(dim=1)).max())
+    del res_inv
+    pinv.close()
+    # Woodbury factorisation + refined solve
+    t0 = time.perf_counter()
+    plan.factor()
+    torch.cuda.synchronize()
+    t_fac = time.perf_counter() - t0
+    W = torch.empty_like(X)
+    info = {}
+
+    def solve():
+        _, info["res"], info["its"] = plan.solve_refined(X, tol=1e-12, maxiter=8, out=W, strict=False,
+                                                         precise=False)
+    ms_solve = _timed(solve, steps, warmup)
+    plan.close()
+    return {
+        "metric": f"PLR product RHS/s (dplrgepdmm, N={n}, rank {C2['rank']}, {nrhs} RHS, FP64)",
+        "value": nrhs / (ms_apply / 1e3), "unit": "RHS/s", "ms_per_step": ms_apply,
+        "higher_is_better": True, "dtype": "f64", "gpu_launches": launches,
+        "roofline": {"kernel": "FP64 apply (panel, reduce, expand)", "bound": "fp64", "achieved": tflops,
+                     "peak": fp64["tflops"], "unit": "TFLOP/s", "frac": tflops / fp64["tflops"],
+                     "traffic": None, "peak_source": "of " + fp64["source"],
+                     "algorithmic": f"2 nnz n = {flops:.4g} flop, 8 nnz + 16 N n = "
+                                    f"{8.0 * plan.nnz + 16.0 * n * nrhs:.4g} bytes"},
+        "config": {"workload": (f"1D exponential kernel (l={C2['ell']}, +{C2['shift']:g} I) PLR, N={n}, leaf "
+                                f"{C2['leaf']}, 9 levels, fixed rank {C2['rank']} (exact rank-1 factor + "
+                                f"round-off tail), {nrhs} standard-normal RHS"),
+                   "nnz": plan.nnz, "l2": "factors (872 MB) larger than L2",
+                   "inverse_apply_explicit": {"ms": ms_inv, "rhs_per_s": nrhs / (ms_inv / 1e3),
+                                              "nnz_inverse": nnz_inv, "geinv_s": t_inv,
+                                              "max_rel_resid_fp64": rel_inv},
+                   "solve_woodbury_refined": {"ms": ms_solve, "rhs_per_s": nrhs / (ms_solve / 1e3),
+                                              "factor_s": t_fac, "rel_resid": info.get("res"),
+                                              "corrections": info.get("its")}},
     }

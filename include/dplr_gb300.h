@@ -150,7 +150,12 @@ DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double
  * the GPU race and must be ordered by the caller; a call needing more
  * scratch than that, (sum of ranks + partial panels) * n doubles, fails
  * with DPLR_GPU_EINVAL.  The first call on a device resolves the array's
- * address and should come before any stream capture. */
+ * address and should come before any stream capture.  That address is kept
+ * for the life of the process: it assumes one CUDA context per device (the
+ * primary context, not reset with cudaDeviceReset in between).  The array's
+ * contents are never read before a call writes them, and its 64 MiB are
+ * reserved on every device where the library's module is loaded, whether or
+ * not this entry point is called. */
 DPLR_API int dplr_gpu_apply_noalloc(dplr_gpu_plan plan, char trans, int n, double alpha,
                                     const double *X, int ldx, double beta, double *Y, int ldy,
                                     void *stream);
@@ -257,7 +262,13 @@ DPLR_API void dplr_gpu_release_staging(void);
 DPLR_API int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers);
 
 /* Associate the drop-in entry points with a plan for this host tree
- * (they then skip the upload).  dplr_gpu_unregister drops the link. */
+ * (they then skip the upload).  dplr_gpu_unregister drops the link.  A
+ * registration is found by the tree's address and size only: unregister
+ * before freeing or reshaping the tree, or a new tree at the same address
+ * would use the old factors.  A drop-in call keeps its registered plan alive
+ * until it returns, so (un)registering from another thread is safe; two
+ * drop-in calls on the same registered tree must not overlap (they share
+ * the plan's device buffers). */
 DPLR_API int dplr_gpu_register(int m, DPlrMtx *A);
 DPLR_API int dplr_gpu_unregister(DPlrMtx *A);
 

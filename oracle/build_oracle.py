@@ -25,7 +25,12 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
+# The reference checkout: $DPLR_REFERENCE_ROOT, else a directory named
+# "reference" beside the repository.  It exists only where the fixtures are
+# made; the GPU machine has none and builds only the restatement.
+REFERENCE_ROOT = os.environ.get(
+    "DPLR_REFERENCE_ROOT",
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 # Fortran BLAS/LAPACK symbols declared by the reference's lapackapi_netlib.h.
 _RENAMED = ["dscal_", "dcopy_", "dnrm2_", "ddot_", "daxpy_", "dgemv_", "dgemm_",
@@ -60,16 +65,18 @@ def _link_flags(lib: str) -> list[str]:
 def build_oracle(verbose: bool = False) -> dict:
     """Compile the oracle libraries; returns their paths."""
     os.makedirs(BUILD, exist_ok=True)
-    cflags = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-Wall"]
-    src = os.path.join(HERE, "dplr_oracle.c")
+    # no contraction of a*b+c into fma: the double-double checker relies
+    # on exact TwoSum steps, and the restatement on the reference's rounding
+    cflags = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-Wall", "-ffp-contract=off", "-pthread"]
+    src = [os.path.join(HERE, "dplr_oracle.c"), os.path.join(HERE, "dd_resid.c")]
     out = {}
     loops = os.path.join(BUILD, "liboracle_loops.so")
-    _run(cflags + [src, os.path.join(HERE, "oblas_naive.c"), "-o", loops, "-lm"])
+    _run(cflags + src + [os.path.join(HERE, "oblas_naive.c"), "-o", loops, "-lm"])
     out["loops"] = loops
     lib = find_scipy_openblas()
     if lib is not None:
         blas = os.path.join(BUILD, "liboracle.so")
-        _run(cflags + [src, os.path.join(HERE, "oblas_scipy.c"), "-o", blas] + _link_flags(lib))
+        _run(cflags + src + [os.path.join(HERE, "oblas_scipy.c"), "-o", blas] + _link_flags(lib))
         out["blas"] = blas
     if verbose:
         print("oracle:", out)

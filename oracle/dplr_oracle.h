@@ -44,6 +44,13 @@ int  orc_dortlr(int nnu, int nnv, double *u, double *v, int lrankini, double *sv
                 double eps, int niter);
 void orc_reduce(int m, DPlrMtx *A, double eps);
 
+/* Checker (not a restatement): rnorm[j] = ||b_j - A x_j||_2 with A x_j
+ * evaluated in double-double arithmetic, absnorm[j] = || |A||x_j| ||_2,
+ * for columns j < ncols, spread over nthreads threads (dd_resid.c).
+ * Returns 0, or -1 on a bad argument or failed allocation. */
+int  orc_resid_dd(int m, DPlrMtx *A, int ncols, const double *X, int ldx, const double *B,
+                  int ldb, double *rnorm, double *absnorm, int nthreads);
+
 /* Number of argument errors reported since load (the reference prints
  * them to stderr and returns without touching outputs). */
 long orc_error_count(void);

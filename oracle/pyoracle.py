@@ -49,6 +49,10 @@ def oracle(kind: str = "best") -> PlrApi:
         lib.orc_error_count.restype = ctypes.c_long
         lib.orc_set_threads.argtypes = [ctypes.c_int]
         lib.orc_blas_optimised.restype = ctypes.c_int
+        lib.orc_resid_dd.restype = ctypes.c_int
+        lib.orc_resid_dd.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, c_double_p,
+                                     ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
+                                     c_double_p, ctypes.c_int]
         api.path = path
         _cache[path] = api
     return _cache[path]
@@ -63,6 +67,24 @@ def dortlr(api: PlrApi, u: np.ndarray, v: np.ndarray, sval: np.ndarray, eps: flo
     return api.lib.orc_dortlr(u.shape[0], v.shape[0], u.ctypes.data_as(c_double_p),
                               v.ctypes.data_as(c_double_p), u.shape[1],
                               sval.ctypes.data_as(c_double_p), eps, niter)
+
+
+def resid_dd(api: PlrApi, cptr, x: np.ndarray, b: np.ndarray, threads: int | None = None):
+    """Per column j of x, b (arrays of shape (ncols, m), row j = column j):
+    (||b_j - A x_j||, || |A||x_j| ||) with A x_j evaluated in double-double
+    arithmetic on the tree `cptr` (a DPlrMtx pointer)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if x.shape != b.shape or x.ndim != 2:
+        raise ValueError("x and b must be (ncols, m) arrays of the same shape")
+    nc, m = x.shape
+    rn, an = np.zeros(nc), np.zeros(nc)
+    rc = api.lib.orc_resid_dd(m, ctypes.cast(cptr, ctypes.c_void_p), nc, x.ctypes.data_as(c_double_p), m,
+                              b.ctypes.data_as(c_double_p), m, rn.ctypes.data_as(c_double_p),
+                              an.ctypes.data_as(c_double_p), int(threads or os.cpu_count() or 1))
+    if rc != 0:
+        raise RuntimeError("orc_resid_dd failed")
+    return rn, an
 
 
 def error_count(api: PlrApi) -> int:

@@ -42,26 +42,48 @@ def test_library_exports_every_declared_symbol():
     assert not missing, f"not exported: {missing}"
 
 
-def test_struct_layout_matches_c():
-    src = r'''
+_LAYOUT_PROBE = r'''
 #include <stdio.h>
 #include <stddef.h>
 #include "dplr.h"
-int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(DPlrMtx), offsetof(DPlrMtx, size),
-  offsetof(DPlrMtx, dlr.rank), offsetof(DPlrMtx, dlr.u), offsetof(DPlrMtx, dlr.sig),
-  offsetof(DPlrMtx, dh.sw)); return 0;}
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(DPlrMtx),
+  offsetof(DPlrMtx, type), offsetof(DPlrMtx, size), offsetof(DPlrMtx, dh.nw),
+  offsetof(DPlrMtx, dh.ne), offsetof(DPlrMtx, dh.se), offsetof(DPlrMtx, dh.sw),
+  offsetof(DPlrMtx, dd.d), offsetof(DPlrMtx, dlr.rank), offsetof(DPlrMtx, dlr.capacity),
+  offsetof(DPlrMtx, dlr.u), offsetof(DPlrMtx, dlr.sig)); return 0;}
 '''
-    tmp = os.path.join(ROOT, "_work")
-    os.makedirs(tmp, exist_ok=True)
-    c = os.path.join(tmp, "layout.c")
-    exe = os.path.join(tmp, "layout")
-    open(c, "w").write(src)
-    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
-    out = [int(v) for v in subprocess.check_output([exe]).split()]
-    D = tree.DPlrMtx
-    assert out == [ctypes.sizeof(D), D.size.offset, D.body.offset + tree._LRPart.rank.offset,
-                   D.body.offset + tree._LRPart.u.offset, D.body.offset + tree._LRPart.sig.offset,
-                   D.body.offset + tree._HPart.sw.offset]
+
+
+def _layout(include_dir: str, tmp_path) -> list[int]:
+    """sizeof/offsetof of DPlrMtx as a C compiler lays it out with the
+    dplr.h found in include_dir."""
+    c = tmp_path / "layout.c"
+    exe = tmp_path / f"layout_{abs(hash(include_dir))}"
+    c.write_text(_LAYOUT_PROBE)
+    subprocess.check_call(["gcc", "-w", "-I", include_dir, str(c), "-o", str(exe)])
+    return [int(v) for v in subprocess.check_output([str(exe)]).split()]
+
+
+def test_struct_layout_matches_c(tmp_path):
+    """The ctypes mirror has the layout of this repository's dplr.h."""
+    out = _layout(os.path.join(ROOT, "include"), tmp_path)
+    D, H, L = tree.DPlrMtx, tree._HPart, tree._LRPart
+    b = D.body.offset
+    assert out[0] == ctypes.sizeof(D)
+    assert out[2] == D.size.offset
+    assert out[3:7] == [b + H.nw.offset, b + H.ne.offset, b + H.se.offset, b + H.sw.offset]
+    assert out[8:12] == [b + L.rank.offset, b + L.capacity.offset, b + L.u.offset, b + L.sig.offset]
+
+
+def test_struct_layout_matches_the_reference_header(tmp_path):
+    """dplr.h here and the reference's include/dplr.h (which pulls in
+    include/dplr_internal.h:32-87) give DPlrMtx the same size and the same
+    offsets for every member, so trees pass between the two unchanged."""
+    from oracle.build_oracle import REFERENCE_ROOT
+    ref_inc = os.path.join(REFERENCE_ROOT, "include")
+    if not os.path.exists(os.path.join(ref_inc, "dplr_internal.h")):
+        pytest.skip("reference headers not present on this machine")
+    assert _layout(os.path.join(ROOT, "include"), tmp_path) == _layout(ref_inc, tmp_path)
 
 
 def test_structure_helpers_on_host():

@@ -1,0 +1,252 @@
+"""The benchmark configurations at their full sizes, checked by the oracle.
+
+* C2: N = 131072, 1D exponential kernel (length 0.05, +1e-2 I), leaf 256,
+  9 levels, fixed rank 32, 64 RHS: the GPU dplrgepdmm against the oracle's
+  (src/dplrpdmm.c:454 restated) at 1e-12; the refined Woodbury solve
+  against the oracle's double-double residual at 1e-12; the GPU dplrgeinv
+  (src/dplrinv.c:93) against the oracle's explicit inverse: identical
+  ranks and capacities, and the same operator applied to the 64 RHS.
+* C4: 512 independent 1D exponential-kernel matrices, N = 64 2^L in
+  [1024, 16384], ranks 1-4, 1-16 RHS each, in one batched plan: every
+  matrix's product against the oracle at 1e-12, every matrix's refined
+  solve against the oracle's double-double residual at 1e-12.
+* C5: N = 65536, leaf 128, rank 16: the gradient of
+  L = ||A^-1 b - t||^2 with respect to b and every stored factor against an
+  FP64 CPU reference gradient built from the oracle (explicit inverse
+  solves refined with its dplrgepdmm; dA = -lambda x^T projected onto the
+  factors), and against central differences (h = 1e-6).
+"""
+import numpy as np
+import pytest
+
+from dplr_gb300 import tree, workloads
+from oracle import pyoracle
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+torch = pytest.importorskip("torch")
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def oracle_solve(orc, a, binv, m, b, trans="N", steps=6):
+    """x = op(A)^-1 b on the host with the reference's algorithm: the
+    explicit inverse binv (from dplrgeinv) applied, then refined with
+    dplrgepdmm of A.  b: (k, m).  Returns x of the same shape."""
+    k = b.shape[0]
+    bf = np.ascontiguousarray(b).reshape(-1)
+    x = np.zeros(m * k)
+    orc.gepdmm(trans, "N", m, k, 1.0, binv, bf, m, 0.0, x, m)
+    r, d = np.empty_like(x), np.empty_like(x)
+    for _ in range(steps):
+        r[:] = bf
+        orc.gepdmm(trans, "N", m, k, -1.0, a, x, m, 1.0, r, m)
+        orc.gepdmm(trans, "N", m, k, 1.0, binv, r, m, 0.0, d, m)
+        x += d
+    return x.reshape(k, m)
+
+
+# ----------------------------------------------------------------------- C2
+
+@pytest.fixture(scope="module")
+def c2():
+    t = workloads.c2_input()
+    a = tree.to_c(t)
+    yield t, a
+    tree.free_c(a)
+
+
+def test_c2_product_matches_oracle(c2):
+    from dplr_gb300.plan import GpuPlan
+    t, a = c2
+    assert tree.nnz(t) == 109051904             # dplrnz of the configuration
+    X = workloads.c2_rhs()
+    plan = GpuPlan(t)
+    Y = plan.apply(X).cpu().numpy()
+    plan.close()
+    orc = pyoracle.oracle("best")
+    want = np.zeros(Y.size)
+    orc.gepdmm("N", "N", t.size, X.shape[0], 1.0, a, X.cpu().numpy().reshape(-1), t.size, 0.0, want, t.size)
+    assert _rel(Y.reshape(-1), want) <= 1e-12
+
+
+def test_c2_refined_solve_checked_by_the_oracle(c2):
+    from dplr_gb300.plan import GpuPlan
+    t, a = c2
+    B = workloads.c2_rhs()
+    plan = GpuPlan(t)
+    plan.factor()
+    X, res, _ = plan.solve_refined(B, tol=1e-12, maxiter=8, precise=False)
+    plan.close()
+    assert res <= 1e-12
+    Bh = B.cpu().numpy()
+    rn, _ = pyoracle.resid_dd(pyoracle.oracle("best"), a, X.cpu().numpy(), Bh)
+    assert np.max(rn / np.linalg.norm(Bh, axis=1)) <= 1e-12
+
+
+def _ranks_caps(node, out=None):
+    out = [] if out is None else out
+    if isinstance(node, tree.HNode):
+        out.append((node.ne.rank, node.ne.capacity, node.sw.rank, node.sw.capacity))
+        _ranks_caps(node.nw, out)
+        _ranks_caps(node.se, out)
+    return out
+
+
+def test_c2_explicit_inverse_matches_oracle(c2):
+    """DPLR's inverse representation at full size: same tree, ranks (32 at
+    the top growing to 288 at the leaves' parents) and capacities; applied
+    to the 64 RHS, the two inverses agree to the accuracy an explicit FP64
+    inverse has (its own residual), and the GPU's residual is no worse than
+    the oracle's."""
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+    t, a = c2
+    m = t.size
+    orc, gpu = pyoracle.oracle("best"), _native.api()
+    bo, bg = tree.new_empty(), tree.new_empty()
+    assert orc.geinv(m, a, bo, 0.0) == 0
+    assert gpu.geinv(m, a, bg, 0.0) == 0
+    to, tg = tree.from_c(bo), tree.from_c(bg)
+    assert _ranks_caps(tg) == _ranks_caps(to)
+    assert orc.nz(m, bg) == orc.nz(m, bo)
+    X = workloads.c2_rhs()
+    Xh = X.cpu().numpy()
+    zo = np.zeros(Xh.size)
+    orc.gepdmm("N", "N", m, Xh.shape[0], 1.0, bo, Xh.reshape(-1), m, 0.0, zo, m)
+    pg = GpuPlan(bg)
+    zg = pg.apply(X).cpu().numpy()
+    pg.close()
+    tree.free_c(bo)
+    tree.free_c(bg)
+    zo = zo.reshape(Xh.shape)
+    rg, _ = pyoracle.resid_dd(orc, a, zg, Xh)
+    ro, _ = pyoracle.resid_dd(orc, a, zo, Xh)
+    bn = np.linalg.norm(Xh, axis=1)
+    res_o = float(np.max(ro / bn))
+    assert float(np.max(rg / bn)) <= 2.0 * res_o + 1e-14
+    # the difference of two FP64 inverses is of the order of their residuals
+    # amplified by ||A^-1||: bounded here by 100x the oracle's own residual
+    assert _rel(zg, zo) <= max(100.0 * res_o, 1e-12)
+
+
+# ----------------------------------------------------------------------- C4
+
+def test_c4_batch_products_and_refined_solves_checked_by_the_oracle():
+    from dplr_gb300.plan import GpuPlan
+    trees, nrhs = workloads.batched_trees(512)
+    plan = GpuPlan.batch(trees)
+    plan.factor()
+    offs = plan.offsets()
+    n = max(nrhs)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    Bh = np.zeros((n, plan.m))
+    for o, tr_, k in zip(offs, trees, nrhs):
+        Bh[:k, o:o + tr_.size] = torch.randn(k, tr_.size, generator=g, dtype=torch.float64).numpy()
+    B = torch.tensor(Bh, device="cuda")
+    Y = plan.apply(B).cpu().numpy()
+    X, res, _ = plan.solve_refined(B, tol=1e-12, maxiter=8, precise=False)
+    plan.close()
+    assert res <= 1e-12
+    Xh = X.cpu().numpy()
+    orc = pyoracle.oracle("best")
+    worst_apply, worst_dd = 0.0, 0.0
+    for o, tr_, k in zip(offs, trees, nrhs):
+        m = tr_.size
+        a = tree.to_c(tr_)
+        b = np.ascontiguousarray(Bh[:k, o:o + m])
+        want = np.zeros(k * m)
+        orc.gepdmm("N", "N", m, k, 1.0, a, b.reshape(-1), m, 0.0, want, m)
+        worst_apply = max(worst_apply, _rel(Y[:k, o:o + m].reshape(-1), want))
+        rn, _ = pyoracle.resid_dd(orc, a, Xh[:k, o:o + m], b)
+        worst_dd = max(worst_dd, float(np.max(rn / np.linalg.norm(b, axis=1))))
+        tree.free_c(a)
+    assert worst_apply <= 1e-12
+    assert worst_dd <= 1e-12
+
+
+# ----------------------------------------------------------------------- C5
+
+def _rank1_pool_grads(blocks, pool, lam, x):
+    """FP64 reference gradient of the factors for dA = -lam x^T (one
+    right-hand side): per low-rank block dU = -lam_R (s o V^T x_C)^T,
+    dV = -x_C (s o U^T lam_R)^T, ds = -(U^T lam_R) o (V^T x_C); per leaf
+    dD = -lam_R x_R^T.  Pool layout as GpuPlan.pool_blocks() gives it."""
+    g = np.zeros_like(pool)
+    for blk in blocks:
+        if blk["kind"] == "lowrank":
+            n, r = blk["n"], blk["rank"]
+            if r == 0:
+                continue
+            u = pool[blk["u"]:blk["u"] + n * r].reshape(r, n).T
+            v = pool[blk["v"]:blk["v"] + n * r].reshape(r, n).T
+            s = pool[blk["sig"]:blk["sig"] + r]
+            lr, xc = lam[blk["row0"]:blk["row0"] + n], x[blk["col0"]:blk["col0"] + n]
+            vx, ul = v.T @ xc, u.T @ lr
+            g[blk["u"]:blk["u"] + n * r] = (-np.outer(lr, s * vx)).T.reshape(-1)
+            g[blk["v"]:blk["v"] + n * r] = (-np.outer(xc, s * ul)).T.reshape(-1)
+            g[blk["sig"]:blk["sig"] + r] = -ul * vx
+        else:
+            b, R = blk["b"], blk["row0"]
+            g[blk["d"]:blk["d"] + b * b] = (-np.outer(lam[R:R + b], x[R:R + b])).T.reshape(-1)
+    return g
+
+
+def test_c5_solve_gradients_against_oracle_reference_and_differences():
+    from dplr_gb300 import gen
+    from dplr_gb300.autograd import plr_solve
+    from dplr_gb300.plan import GpuPlan
+    n = 65536
+    rng = np.random.default_rng(0)
+    pts = np.sort(rng.uniform(0.0, 1.0, n))
+    t = gen.exp1d_tree(pts, ell=0.1, shift=1e-2, leaf=128, rank=16, seed=1)
+    b = rng.standard_normal((1, n))
+    tt = rng.standard_normal((1, n))
+    plan = GpuPlan(t)
+    pool0 = plan.read_pool()
+    pool = pool0.clone().requires_grad_()
+    bt = torch.tensor(b, device="cuda", requires_grad=True)
+    xg = plr_solve(plan, pool, bt)
+    ttc = torch.tensor(tt, device="cuda")
+    loss = ((xg - ttc) ** 2).sum()
+    loss.backward()
+    gpool, gb = pool.grad.cpu().numpy(), bt.grad.cpu().numpy()
+
+    # FP64 CPU reference: x = A^-1 b, lam = A^-T 2 (x - t) by the oracle
+    orc = pyoracle.oracle("best")
+    a, binv = tree.to_c(t), tree.new_empty()
+    assert orc.geinv(n, a, binv, 0.0) == 0
+    x = oracle_solve(orc, a, binv, n, b)
+    lam = oracle_solve(orc, a, binv, n, 2.0 * (x - tt), trans="T")
+    tree.free_c(binv)
+    tree.free_c(a)
+    lref = float(np.sum((x - tt) ** 2))
+    gref = _rank1_pool_grads(plan.pool_blocks(), pool0.cpu().numpy(), lam[0], x[0])
+    assert abs(float(loss) - lref) <= 1e-9 * abs(lref)
+    assert np.max(np.abs(gb - lam)) <= 1e-8 * np.max(np.abs(lam))
+    assert np.max(np.abs(gpool - gref)) <= 1e-8 * np.max(np.abs(gref))
+
+    # central differences on a few factor entries and one entry of b
+    blocks = plan.pool_blocks()
+    lrb = [blk for blk in blocks if blk["kind"] == "lowrank"]
+    lfb = [blk for blk in blocks if blk["kind"] == "leaf"]
+    idx = [lrb[0]["u"] + 5, lrb[1]["sig"], lrb[len(lrb) // 2]["v"] + 9, lfb[3]["d"] + 2 + 5 * lfb[3]["b"]]
+    h = 1e-6
+
+    def loss_at(p, bb):
+        with torch.no_grad():
+            return float(((plr_solve(plan, p, torch.tensor(bb, device="cuda")) - ttc) ** 2).sum())
+
+    for i in idx:
+        pp, pm = pool0.clone(), pool0.clone()
+        pp[i] += h
+        pm[i] -= h
+        fd = (loss_at(pp, b) - loss_at(pm, b)) / (2 * h)
+        assert abs(fd - gpool[i]) <= 1e-5 * max(1.0, abs(gpool[i])), (i, fd, gpool[i])
+    bp, bm = b.copy(), b.copy()
+    bp[0, 1234] += h
+    bm[0, 1234] -= h
+    fd = (loss_at(pool0, bp) - loss_at(pool0, bm)) / (2 * h)
+    assert abs(fd - gb[0, 1234]) <= 1e-5 * max(1.0, abs(gb[0, 1234]))
+    plan.close()
