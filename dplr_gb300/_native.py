@@ -92,7 +92,9 @@ def _bind(lib: ctypes.CDLL) -> None:
 
 
 # Entry points added by later modules of the library (bound when present).
-_OPTIONAL: list = []
+_OPTIONAL: list = [
+    ("dplr_gpu_debug_fail_alloc", None, [c_int]),
+]
 
 
 def lib() -> ctypes.CDLL:

@@ -12,6 +12,8 @@
 // rows of op(B) are rejected (DPLR reads out of bounds for them).
 #include "internal.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -119,6 +121,7 @@ const char *dplr_gpu_last_error(void) { return dg::last_error_c(); }
 
 int dplr_gpu_plan_create(int m, const DPlrMtx *A, void *stream, dplr_gpu_plan *plan)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_plan_create");
     if (!plan) return fail(DPLR_GPU_EINVAL, "dplr_gpu_plan_create: null output");
     Plan *p = nullptr;
     int rc = plan_build(m, A, (cudaStream_t)stream, &p);
@@ -163,6 +166,7 @@ int dplr_gpu_prepare_pairs(dplr_gpu_plan plan, void *stream)
 int dplr_gpu_apply(dplr_gpu_plan plan, char trans, int n, double alpha, const double *X, int ldx,
                    double beta, double *Y, int ldy, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_apply");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_apply: null plan");
     if (n < 0 || ldx < (p->m > 0 ? p->m : 1) || ldy < (p->m > 0 ? p->m : 1))
@@ -203,6 +207,7 @@ int dplr_gpu_unregister(DPlrMtx *A)
 void dplrgepmv(char trans, int m, double *alpha, DPlrMtx *A, double *x, int incx, double *beta,
                double *y, int incy)
 {
+    dg::NvtxRange nvtx_("dplrgepmv");
     const char *fn = "dplrgepmv";
     if (m < 0) {
         fail(DPLR_GPU_EINVAL, "invalid matrix size %d", m);
@@ -236,6 +241,7 @@ void dplrgepmv(char trans, int m, double *alpha, DPlrMtx *A, double *x, int incx
 void dplrgepdmm(char transa, char transb, int m, int n, double *alpha, DPlrMtx *A, double *B,
                 int ldb, double *beta, double *C, int ldc)
 {
+    dg::NvtxRange nvtx_("dplrgepdmm");
     const char *fn = "dplrgepdmm";
     int ta = !(transa == 'N' || transa == 'n');
     int tb = !(transb == 'N' || transb == 'n');
@@ -304,6 +310,32 @@ static std::vector<ProfAgg> g_prof_out;
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void note_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
+// Allocation-failure injection: countdown of allocations that still
+// succeed; -1 = off.  Armed from DPLR_GB300_FAIL_ALLOC at load, or by
+// dplr_gpu_debug_fail_alloc.  The failing allocation makes no CUDA call.
+static std::atomic<long long> g_fail_countdown{[] {
+    const char *v = getenv("DPLR_GB300_FAIL_ALLOC");
+    return v && *v ? atoll(v) : -1LL;
+}()};
+
+cudaError_t dev_malloc(void **ptr, size_t bytes)
+{
+    long long c = g_fail_countdown.load();
+    while (c >= 0) {
+        if (g_fail_countdown.compare_exchange_weak(c, c - 1)) {
+            if (c == 0) {
+                *ptr = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(ptr, bytes);
+}
+
+NvtxRange::NvtxRange(const char *name) { nvtxRangePushA(name); }
+NvtxRange::~NvtxRange() { nvtxRangePop(); }
+
 ProfScope::ProfScope(const char *name, cudaStream_t st, double flops, double bytes)
 {
     if (!g_prof_on.load()) return;
@@ -328,6 +360,8 @@ ProfScope::~ProfScope()
 extern "C" {
 
 long long dplr_gpu_launch_count(void) { return dg::g_launches.load(); }
+
+void dplr_gpu_debug_fail_alloc(int after) { dg::g_fail_countdown.store(after < 0 ? -1 : after); }
 
 int dplr_gpu_profile_start(void)
 {

@@ -17,6 +17,8 @@
 #include "internal.cuh"
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 namespace dg {
 
@@ -625,6 +627,11 @@ int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, in
         return rc;
     }
     if (pairs_usable(p, trans, nrhs)) return pairs_apply(p, alpha, X, beta, Y, st);
+    // one persistent launch unless DPLR_GB300_APPLY=launches asks for the
+    // three-launch form (panel, reduce, expand)
+    const char *mode = getenv("DPLR_GB300_APPLY");
+    if (!(mode && !strcmp(mode, "launches")) && persist_usable(p, trans, nrhs))
+        return persist_apply(p, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
     const Schedule &S = p->sched[trans ? 1 : 0];
     size_t need = (size_t)(S.t_per_rhs + S.partial_per_rhs) * nrhs;
     int rc = ensure_buffer(&p->work, &p->work_doubles, need);

@@ -48,6 +48,7 @@ extern "C" {
 
 int dplr_gpu_batch_create(int count, const int *m, DPlrMtx *const *A, void *stream, dplr_gpu_plan *plan)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_batch_create");
     if (!plan || count <= 0 || !m || !A) return fail(DPLR_GPU_EINVAL, "dplr_gpu_batch_create: invalid arguments");
     *plan = nullptr;
     for (int i = 0; i < count; ++i)
@@ -72,6 +73,7 @@ int dplr_gpu_batch_offsets(dplr_gpu_plan plan, int *count, int *row0)
 int dplr_gpu_graph_create(dplr_gpu_plan plan, char op, char trans, int n, const double *X, int ldx, double *Y,
                           int ldy, void *stream, dplr_gpu_graph *graph)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_graph_create");
     Plan *p = (Plan *)plan;
     if (!p || !graph) return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: null argument");
     *graph = nullptr;

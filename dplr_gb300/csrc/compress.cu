@@ -40,6 +40,10 @@
 
 namespace dg {
 int fail(int code, const char *fmt, ...);
+struct NvtxRange {
+    explicit NvtxRange(const char *name);
+    ~NvtxRange();
+};
 void note_launch();
 void note_launches(long long k);
 int validate_tree(int m, const DPlrMtx *A, const char *fn);
@@ -569,6 +573,7 @@ extern "C" {
 
 int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int nlvl, int workers, int *info)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_d2gep");
     *info = -1;
     if (m < 0) {
         fprintf(stderr, "dplrd2gep: invalid matrix size %d\n", m);
@@ -666,6 +671,7 @@ int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int 
 
 int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_reduce_svd");
     const char *fn = "dplr_gpu_reduce_svd";
     if (m < 0) return dg::fail(DPLR_GPU_EINVAL, "%s: invalid matrix size %d", fn, m);
     if (!A) return dg::fail(DPLR_GPU_EINVAL, "%s: null argument", fn);
@@ -712,6 +718,7 @@ int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers)
 
 void dplrd2gep(int m, double *A, int lda, DPlrMtx *B, double eps, int nlvl, int *info)
 {
+    dg::NvtxRange nvtx_("dplrd2gep");
     dplr_gpu_d2gep(m, A, lda, B, eps, nlvl, 0, info);
 }
 

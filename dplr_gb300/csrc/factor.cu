@@ -173,7 +173,7 @@ template <class T>
 static int to_device(const std::vector<T> &v, T **dst, long long *bytes)
 {
     size_t n = std::max<size_t>(v.size(), 1);
-    DG_CUDA(cudaMalloc((void **)dst, n * sizeof(T)));
+    DG_ALLOC(dst, n * sizeof(T));
     *bytes += (long long)(n * sizeof(T));
     if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return 0;
@@ -195,7 +195,7 @@ static int batched_inverse(double *base, long long *d_off, int *d_size, int coun
 {
     if (count == 0) return 0;
     double *work = nullptr;
-    DG_CUDA(cudaMalloc((void **)&work, std::max<long long>(span, 1) * sizeof(double)));
+    DG_ALLOC(&work, std::max<long long>(span, 1) * sizeof(double));
     lu_inverse_kernel<<<count, 256, 0, st>>>(base, d_off, d_size, work, d_info);
     note_launch();
     cudaError_t e = cudaGetLastError();
@@ -474,7 +474,7 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
 
     int rc;
     auto alloc = [&](double **ptr, long long n) -> int {
-        cudaError_t e = cudaMalloc((void **)ptr, std::max<long long>(n, 1) * sizeof(double));
+        cudaError_t e = dev_malloc((void **)ptr, std::max<long long>(n, 1) * sizeof(double));
         if (e != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "factorisation: cannot allocate %lld doubles", n);
         F->bytes += std::max<long long>(n, 1) * 8;

@@ -256,6 +256,7 @@ int dplr_gpu_pool_write(dplr_gpu_plan plan, const double *src, void *stream)
 int dplr_gpu_grad_factors(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *DY, int ldy,
                           double alpha, double *G, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_grad_factors");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_grad_factors: null plan");
     const int mm = std::max(p->m, 1);

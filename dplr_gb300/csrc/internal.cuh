@@ -32,6 +32,28 @@ int fail(int code, const char *fmt, ...);
                               cudaGetErrorString(e_), __FILE__, __LINE__);         \
     } while (0)
 
+// Device allocations of plans, factorisations and scratch go through
+// dev_malloc, so that a test can make the k-th of them fail
+// (dplr_gpu_debug_fail_alloc, or DPLR_GB300_FAIL_ALLOC=k in the environment
+// when the library loads) and check that every caller reports
+// DPLR_GPU_ENOMEM and leaves its outputs untouched.
+cudaError_t dev_malloc(void **ptr, size_t bytes);
+#define DG_ALLOC(ptr, bytes)                                                                     \
+    do {                                                                                         \
+        cudaError_t e_ = ::dg::dev_malloc((void **)(ptr), (bytes));                             \
+        if (e_ != cudaSuccess)                                                                   \
+            return ::dg::fail(DPLR_GPU_ENOMEM, "cannot allocate %zu bytes of device memory: %s " \
+                              "(%s:%d)", (size_t)(bytes), cudaGetErrorString(e_), __FILE__,      \
+                              __LINE__);                                                        \
+    } while (0)
+
+// NVTX range around an entry point (visible in Nsight tools; a no-op unless
+// a tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name);
+    ~NvtxRange();
+};
+
 // ------------------------------------------------------- instrumentation
 // Every kernel launch of the library is counted; when profiling is on, the
 // main launch sites also bracket their launch with CUDA events on the
@@ -126,6 +148,9 @@ struct Schedule {
     int *d_tile_row0 = nullptr, *d_tile_begin = nullptr;
     TileTerm *d_terms = nullptr;
     CapItem *d_caps = nullptr;
+    // persistent apply (persist.cu): reduce index of every panel item and
+    // of every tile term that reads T (-1: leaf term), built on first use
+    int *d_item_red = nullptr, *d_term_red = nullptr;
 };
 
 struct Plan {
@@ -198,6 +223,14 @@ int run_cap_list(const std::vector<CapItem> &caps, const CapItem *d_caps, const 
 int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx,
                  double beta, double *Y, int ldy, cudaStream_t st, bool alpha0_squares_beta);
 int scale_device(double *Y, int rows, int cols, int ldy, double beta, cudaStream_t st);
+
+// persist.cu: the whole FP64 apply in one persistent launch
+bool persist_usable(const Plan *p, int trans, int nrhs);
+int persist_apply(Plan *p, int trans, int nrhs, double alpha, const double *X, int ldx, double beta, double *Y,
+                  int ldy, cudaStream_t st);
+// sliced.cu: the plan's mapped error flag of kernels with bounded waits
+int ensure_err_flag(Plan *p);
+int sliced_error(Plan *p);
 
 // pairs.cu: FP64-accurate 1-RHS apply on the FP32 pipes
 int pairs_prepare(Plan *p, cudaStream_t st);

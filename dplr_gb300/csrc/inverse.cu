@@ -136,7 +136,7 @@ static long long al32(long long x) { return (x + 31) & ~31LL; }
 template <class T>
 static int vec_to_dev(const std::vector<T> &v, T **dst)
 {
-    DG_CUDA(cudaMalloc((void **)dst, std::max<size_t>(v.size(), 1) * sizeof(T)));
+    DG_ALLOC(dst, std::max<size_t>(v.size(), 1) * sizeof(T));
     if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return 0;
 }
@@ -149,7 +149,7 @@ struct DevBuf {
     }
     int alloc(double **p, long long n)
     {
-        cudaError_t e = cudaMalloc((void **)p, std::max<long long>(n, 1) * sizeof(double));
+        cudaError_t e = dev_malloc((void **)p, std::max<long long>(n, 1) * sizeof(double));
         if (e != cudaSuccess) return fail(DPLR_GPU_ENOMEM, "geinv: cannot allocate %lld doubles", n);
         ptrs.push_back(*p);
         return 0;
@@ -542,6 +542,7 @@ using namespace dg;
 
 extern "C" void dplrgeinv(int m, DPlrMtx *A, DPlrMtx *B, double eps, int *info)
 {
+    dg::NvtxRange nvtx_("dplrgeinv");
     const char *fn = "dplrgeinv";
     if (m < 0) {
         fprintf(stderr, "%s: invalid matrix size: %d\n", fn, m);
@@ -620,6 +621,7 @@ __global__ void leaf_rank_update_kernel(const LeafJob *__restrict__ jobs,
 extern "C" void dplrgeprk(int m, int k, double *alpha, double *u, int ldu, double *v, int ldv,
                           double *s, int incs, DPlrMtx *A, double eps)
 {
+    dg::NvtxRange nvtx_("dplrgeprk");
     const char *fn = "dplrgeprk";
     if (m < 0) {
         fprintf(stderr, "%s: invalid matrix size %d\n", fn, m);

@@ -71,6 +71,7 @@ extern "C" int dplr_gpu_apply_noalloc(dplr_gpu_plan plan, char trans, int n, dou
                                       const double *X, int ldx, double beta, double *Y, int ldy,
                                       void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_apply_noalloc");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_apply_noalloc: null plan");
     if (n < 0 || ldx < (p->m > 0 ? p->m : 1) || ldy < (p->m > 0 ? p->m : 1))

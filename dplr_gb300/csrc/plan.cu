@@ -259,7 +259,7 @@ template <class T>
 static int upload_vec(const std::vector<T> &v, T **dst, long long *bytes)
 {
     size_t n = std::max<size_t>(v.size(), 1);
-    DG_CUDA(cudaMalloc((void **)dst, n * sizeof(T)));
+    DG_ALLOC(dst, n * sizeof(T));
     *bytes += (long long)(n * sizeof(T));
     if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return 0;
@@ -364,7 +364,7 @@ int plan_build_forest(int count, const int *ms, const DPlrMtx *const *As, cudaSt
     build_schedule(p, 1, p->sched[1]);
     long long bytes = 0;
     size_t pool_bytes = (size_t)std::max<long long>(p->pool_doubles, 1) * sizeof(double);
-    cudaError_t e = cudaMalloc((void **)&p->pool, pool_bytes);
+    cudaError_t e = dev_malloc((void **)&p->pool, pool_bytes);
     if (e != cudaSuccess) {
         plan_free(p);
         return fail(DPLR_GPU_ENOMEM, "plan: cannot allocate %zu bytes of factor pool: %s",
@@ -412,6 +412,9 @@ void free_schedule(Schedule &S)
     cudaFree(S.d_tile_begin);
     cudaFree(S.d_terms);
     cudaFree(S.d_caps);
+    cudaFree(S.d_item_red);
+    cudaFree(S.d_term_red);
+    S.d_item_red = S.d_term_red = nullptr;
     S.d_items = nullptr;
     S.d_reduces = nullptr;
     S.d_tile_row0 = S.d_tile_begin = nullptr;
@@ -451,7 +454,7 @@ int ensure_buffer(double **buf, size_t *have, size_t need)
     *buf = nullptr;
     *have = 0;
     size_t n = std::max<size_t>(need, 1);
-    cudaError_t e = cudaMalloc((void **)buf, n * sizeof(double));
+    cudaError_t e = dev_malloc((void **)buf, n * sizeof(double));
     if (e != cudaSuccess)
         return fail(DPLR_GPU_ENOMEM, "cannot allocate %zu bytes of device scratch: %s",
                     n * sizeof(double), cudaGetErrorString(e));

@@ -697,6 +697,7 @@ extern "C" {
 int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlrMtx *A, DPlrMtx *B, double beta, DPlrMtx *C,
                     double eps, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_geppmm");
     const int ta = transa == 'T' || transa == 't';
     const int tb = transb == 'T' || transb == 't';
     const char *fn = variant_name(ta, tb);
@@ -723,6 +724,7 @@ void dplr_gpu_release_staging(void)
 void dplrgeppmm(char transa, char transb, int m, double *alpha, DPlrMtx *A, DPlrMtx *B, double *beta, DPlrMtx *C,
                 double eps)
 {
+    dg::NvtxRange nvtx_("dplrgeppmm");
     if (dplr_gpu_geppmm(transa, transb, m, *alpha, A, B, *beta, C, eps, nullptr))
         fprintf(stderr, "%s\n", dplr_gpu_last_error());
 }

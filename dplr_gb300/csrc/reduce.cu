@@ -160,6 +160,7 @@ using namespace dg;
 
 extern "C" void dplrreduce(int m, DPlrMtx *A, double eps)
 {
+    dg::NvtxRange nvtx_("dplrreduce");
     const char *fn = "dplrreduce";
     if (m < 0) {
         fprintf(stderr, "%s: invalid matrix size %d\n", fn, m);

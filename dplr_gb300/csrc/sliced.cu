@@ -701,7 +701,7 @@ static int sliced_tile_rows(const Plan *p)
     return tc::M;
 }
 
-static int ensure_err_flag(Plan *p)
+int ensure_err_flag(Plan *p)
 {
     if (p->tc_err_h) return 0;
     if (cudaHostAlloc((void **)&p->tc_err_h, sizeof(int), cudaHostAllocMapped) != cudaSuccess)
@@ -751,7 +751,7 @@ static void launch_expand(const Plan *p, const SSchedule &S, const bf16 *apool, 
 template <class T>
 static int dev_vec(const std::vector<T> &v, T **dst, long long *bytes)
 {
-    DG_CUDA(cudaMalloc((void **)dst, std::max<size_t>(v.size(), 1) * sizeof(T)));
+    DG_ALLOC(dst, std::max<size_t>(v.size(), 1) * sizeof(T));
     *bytes += (long long)(std::max<size_t>(v.size(), 1) * sizeof(T));
     if (!v.empty()) DG_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return 0;
@@ -857,7 +857,7 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
         nrows += L.b;
     }
     S->stride = al32(std::max<long long>(el, 1));
-    cudaError_t e = cudaMalloc((void **)&S->pool, (size_t)ns * S->stride * sizeof(bf16));
+    cudaError_t e = dev_malloc((void **)&S->pool, (size_t)ns * S->stride * sizeof(bf16));
     if (e != cudaSuccess) return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate slices");
     S->bytes += (long long)ns * S->stride * 2;
     S->nexp = nexp;
@@ -990,14 +990,14 @@ static int sliced_scratch(Sliced *S, const SSchedule &A, int m, int nrhs, int ns
         cudaFree(S->xs);
         S->xs = nullptr;
         S->xs_elems = 0;
-        if (cudaMalloc((void **)&S->xs, xs_need * sizeof(bf16)) != cudaSuccess)
+        if (dev_malloc((void **)&S->xs, xs_need * sizeof(bf16)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate X slices");
         S->xs_elems = xs_need;
     }
     if (S->xexp_n < (size_t)nrhs) {
         cudaFree(S->xexp);
         S->xexp = nullptr;
-        if (cudaMalloc((void **)&S->xexp, nrhs * sizeof(int)) != cudaSuccess)
+        if (dev_malloc((void **)&S->xexp, nrhs * sizeof(int)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
         S->xexp_n = nrhs;
     }
@@ -1238,7 +1238,7 @@ int mixed_build(Plan *p, int ns, cudaStream_t st, bool fp64_caps)
         lj.push_back(RowSliceJob{F->leafoff[i], ls_off[i], L.b, L.b, L.b, L.b, el_off[i]});
     }
     M->stride = al32(std::max<long long>(el, 1));
-    if (cudaMalloc((void **)&M->pool, (size_t)ns * M->stride * sizeof(bf16)) != cudaSuccess)
+    if (dev_malloc((void **)&M->pool, (size_t)ns * M->stride * sizeof(bf16)) != cudaSuccess)
         return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
     M->bytes += (long long)ns * M->stride * 2;
     int rc;
@@ -1365,14 +1365,14 @@ static int mixed_scratch(MixedSliced *M, int m, int nrhs, MWork &w)
         cudaFree(M->xs);
         M->xs = nullptr;
         M->xs_elems = 0;
-        if (cudaMalloc((void **)&M->xs, xs_need * sizeof(bf16)) != cudaSuccess)
+        if (dev_malloc((void **)&M->xs, xs_need * sizeof(bf16)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
         M->xs_elems = xs_need;
     }
     if (M->xexp_n < (size_t)nrhs) {
         cudaFree(M->xexp);
         M->xexp = nullptr;
-        if (cudaMalloc((void **)&M->xexp, nrhs * sizeof(int)) != cudaSuccess)
+        if (dev_malloc((void **)&M->xexp, nrhs * sizeof(int)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate exponents");
         M->xexp_n = nrhs;
     }
@@ -1834,14 +1834,14 @@ int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_
         cudaFree(xs);
         xs = nullptr;
         xs_elems = 0;
-        if (cudaMalloc((void **)&xs, need * sizeof(bf16)) != cudaSuccess)
+        if (dev_malloc((void **)&xs, need * sizeof(bf16)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate X slices");
         xs_elems = need;
     }
     if (xexp_n < (size_t)nrhs) {
         cudaFree(xexp);
         xexp = nullptr;
-        if (cudaMalloc((void **)&xexp, nrhs * sizeof(int)) != cudaSuccess)
+        if (dev_malloc((void **)&xexp, nrhs * sizeof(int)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate exponents");
         xexp_n = nrhs;
     }
@@ -1968,7 +1968,7 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
         nlrows += L.b;
     }
     S->stride = al32(std::max<long long>(el, 1));
-    if (cudaMalloc((void **)&S->pool, (size_t)kNS * S->stride * sizeof(bf16)) != cudaSuccess)
+    if (dev_malloc((void **)&S->pool, (size_t)kNS * S->stride * sizeof(bf16)) != cudaSuccess)
         return fail(DPLR_GPU_ENOMEM, "sliced products: cannot allocate slices");
     S->bytes += (long long)kNS * S->stride * 2;
     DG_CUDA(cudaMemsetAsync(S->pool, 0, (size_t)kNS * S->stride * sizeof(bf16), st));
@@ -2056,7 +2056,7 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     A.tile_begin.push_back((int)A.xterms.size());
     if ((rc = upload_tb(A, &S->bytes))) return rc;
     if (ntiles > 0) {
-        DG_CUDA(cudaMalloc((void **)&A.d_rmax, (size_t)ntiles * tc2::M * sizeof(int)));
+        DG_ALLOC(&A.d_rmax, (size_t)ntiles * tc2::M * sizeof(int));
         S->bytes += (long long)ntiles * tc2::M * sizeof(int);
         tile_rmax_kernel<<<ntiles, tc2::M, 0, st>>>(A.d_xterms, A.d_tile_begin, ntiles, S->exps, A.d_rmax);
         note_launch();
@@ -2197,7 +2197,7 @@ static int build_tc_caps(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
     }
     if (kj.empty()) return 0;
     M->kstride = al32(kel);
-    if (cudaMalloc((void **)&M->kslices, (size_t)kNS * M->kstride * sizeof(bf16)) != cudaSuccess)
+    if (dev_malloc((void **)&M->kslices, (size_t)kNS * M->kstride * sizeof(bf16)) != cudaSuccess)
         return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate capacitance slices");
     M->bytes += (long long)kNS * M->kstride * 2;
     if ((rc = dev_vec(std::vector<int>(kexp, 0), &M->kexps, &M->bytes))) return rc;
@@ -2263,7 +2263,7 @@ static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
         lr += L.b;
     }
     M->stride = al32(std::max<long long>(el, 1));
-    if (cudaMalloc((void **)&M->pool, (size_t)NS * M->stride * sizeof(bf16)) != cudaSuccess)
+    if (dev_malloc((void **)&M->pool, (size_t)NS * M->stride * sizeof(bf16)) != cudaSuccess)
         return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate slices");
     M->bytes += (long long)NS * M->stride * 2;
     DG_CUDA(cudaMemsetAsync(M->pool, 0, (size_t)NS * M->stride * sizeof(bf16), st));
@@ -2410,7 +2410,7 @@ static int mixed_solve_tb(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doub
         cudaFree(M->xexp2);
         M->xexp2 = nullptr;
         M->xexp2_n = 0;
-        if (cudaMalloc((void **)&M->xexp2, nrhs * sizeof(int)) != cudaSuccess)
+        if (dev_malloc((void **)&M->xexp2, nrhs * sizeof(int)) != cudaSuccess)
             return fail(DPLR_GPU_ENOMEM, "mixed solve: cannot allocate exponents");
         M->xexp2_n = nrhs;
     }

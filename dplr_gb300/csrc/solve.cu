@@ -80,6 +80,7 @@ extern "C" {
 
 int dplr_gpu_factor(dplr_gpu_plan plan, int flags, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_factor");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_factor: null plan");
     return factor_build(p, flags, (cudaStream_t)stream);
@@ -88,6 +89,7 @@ int dplr_gpu_factor(dplr_gpu_plan plan, int flags, void *stream)
 int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int ldb, double *X,
                    int ldx, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_solve");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve: null plan");
     if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1))
@@ -99,6 +101,7 @@ int dplr_gpu_solve(dplr_gpu_plan plan, char trans, int n, const double *B, int l
 
 int dplr_gpu_prepare_sliced(dplr_gpu_plan plan, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_prepare_sliced");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_sliced: null plan");
     return sliced_build(p, 8, (cudaStream_t)stream);
@@ -111,6 +114,7 @@ int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream)
 
 int dplr_gpu_prepare_mixed_caps(dplr_gpu_plan plan, int slices, int fp64_capacitance, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_prepare_mixed_caps");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_prepare_mixed: null plan");
     return mixed_build(p, slices, (cudaStream_t)stream, fp64_capacitance != 0);
@@ -119,6 +123,7 @@ int dplr_gpu_prepare_mixed_caps(dplr_gpu_plan plan, int slices, int fp64_capacit
 int dplr_gpu_residual(dplr_gpu_plan plan, int n, const double *X, int ldx, const double *B, int ldb,
                       double *R, int ldr, int flags, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_residual");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_residual: null plan");
     const int mm = std::max(p->m, 1);
@@ -137,6 +142,7 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
                            double tol, int maxiter, int flags, double *rel_resid, int *iters,
                            void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_solve_refined");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: null plan");
     if (!p->fact) return fail(DPLR_GPU_ESTATE, "dplr_gpu_solve_refined: plan is not factored");
@@ -205,6 +211,7 @@ int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int 
                                 int ldx, double tol, int maxiter, int flags, double *rel_resid,
                                 int *iters, void *stream)
 {
+    dg::NvtxRange nvtx_("dplr_gpu_solve_refined_host");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: null plan");
     if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1))

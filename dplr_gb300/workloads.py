@@ -99,21 +99,37 @@ def apply_workload(plan: GpuPlan, n: int, steps: int, warmup: int, root: str) ->
         g = torch.Generator(device="cuda").manual_seed(11)
         X = torch.randn(nrhs, n, generator=g, dtype=torch.float64, device="cuda")
         Y = torch.empty_like(X)
-        for _ in range(max(3, warmup)):
-            plan.apply(X, out=Y)
-        torch.cuda.synchronize()
-        e0, e1 = _events()
-        e0.record(stream)
-        for _ in range(steps):
-            plan.apply(X, out=Y)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
         by = 8.0 * plan.nnz + 16.0 * n * nrhs
         fl = 2.0 * plan.nnz * nrhs
-        rows[nrhs] = {"ms": ms, "gbs": by / (ms / 1e3) / 1e9, "tflops": fl / (ms / 1e3) / 1e12,
-                      "frac_hbm": by / (ms / 1e3) / 1e9 / hbm, "frac_fp64": fl / (ms / 1e3) / 1e12 / fp64,
-                      "autotune": tune}
+        for mode in ("persistent", "launches"):
+            # the default is one persistent launch; DPLR_GB300_APPLY=launches
+            # selects the panel / reduce / expand launches
+            if mode == "launches":
+                os.environ["DPLR_GB300_APPLY"] = "launches"
+            try:
+                for _ in range(max(3, warmup)):
+                    plan.apply(X, out=Y)
+                torch.cuda.synchronize()
+                l0 = _native.launch_count()
+                e0, e1 = _events()
+                e0.record(stream)
+                for _ in range(steps):
+                    plan.apply(X, out=Y)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / steps
+                launches = (_native.launch_count() - l0) / steps
+            finally:
+                os.environ.pop("DPLR_GB300_APPLY", None)
+            rec = {"ms": ms, "gbs": by / (ms / 1e3) / 1e9, "tflops": fl / (ms / 1e3) / 1e12,
+                   "frac_hbm": by / (ms / 1e3) / 1e9 / hbm, "frac_fp64": fl / (ms / 1e3) / 1e12 / fp64,
+                   # roofline of min(HBM, FP64): the slower of moving the bytes and doing the flops
+                   "frac_roofline": max(by / (hbm * 1e9), fl / (fp64 * 1e12)) / (ms / 1e3),
+                   "launches_per_apply": launches, "autotune": tune}
+            if mode == "persistent":
+                rows[nrhs] = rec
+            else:
+                rows[nrhs]["three_launches"] = rec
     one = rows[1]
     # FP64-accurate 1-RHS apply on the FP32 pipes (float-pair copy of the
     # factors); the FP64 kernels' result on the same vector is the reference
@@ -607,12 +623,13 @@ def c2_workload(t, steps: int, warmup: int, root: str) -> dict:
     plan.factor()
     torch.cuda.synchronize()
     t_fac = time.perf_counter() - t0
+    plan.prepare_sliced()                    # FP64 residuals stall near 4e-12 on this matrix
     W = torch.empty_like(X)
     info = {}
 
     def solve():
         _, info["res"], info["its"] = plan.solve_refined(X, tol=1e-12, maxiter=8, out=W, strict=False,
-                                                         precise=False)
+                                                         precise=True)
     ms_solve = _timed(solve, steps, warmup)
     plan.close()
     return {

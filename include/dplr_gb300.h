@@ -229,6 +229,14 @@ DPLR_API int dplr_gpu_autotune(dplr_gpu_plan plan, int n, void *stream, int *chu
  * kernel kinds, whose totals (milliseconds, algorithmic flops and bytes,
  * launches) dplr_gpu_profile_entry() reports. */
 DPLR_API long long dplr_gpu_launch_count(void);
+/* Fault injection for tests: the next `after` device allocations of plans,
+ * factorisations and scratch succeed and the one after fails as if the
+ * device were out of memory (then injection is off again); after < 0 turns
+ * it off.  DPLR_GB300_FAIL_ALLOC=<after> in the environment arms it when
+ * the library loads.  Every entry point then returns DPLR_GPU_ENOMEM (the
+ * drop-ins print their message) and leaves its outputs untouched.  No
+ * counterpart in DPLR. */
+DPLR_API void dplr_gpu_debug_fail_alloc(int after);
 DPLR_API int dplr_gpu_profile_start(void);
 DPLR_API int dplr_gpu_profile_stop(void);
 DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double *flops,

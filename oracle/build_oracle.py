@@ -68,7 +68,7 @@ def build_oracle(verbose: bool = False) -> dict:
     # no contraction of a*b+c into fma: the double-double checker relies
     # on exact TwoSum steps, and the restatement on the reference's rounding
     cflags = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-Wall", "-ffp-contract=off", "-pthread"]
-    src = [os.path.join(HERE, "dplr_oracle.c"), os.path.join(HERE, "dd_resid.c")]
+    src = [os.path.join(HERE, f) for f in ("dplr_oracle.c", "dd_resid.c", "shape.c")]
     out = {}
     loops = os.path.join(BUILD, "liboracle_loops.so")
     _run(cflags + src + [os.path.join(HERE, "oblas_naive.c"), "-o", loops, "-lm"])

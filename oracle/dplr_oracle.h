@@ -51,6 +51,12 @@ void orc_reduce(int m, DPlrMtx *A, double eps);
 int  orc_resid_dd(int m, DPlrMtx *A, int ncols, const double *X, int ldx, const double *B,
                   int ldb, double *rnorm, double *absnorm, int nthreads);
 
+/* Timing stand-in (not a restatement): B := a tree with the structure
+ * DPLR's dplrgeinv gives inv(A) (own rank + the ranks of the ancestors'
+ * corrections in every block, leaves unchanged), every entry `fill`
+ * (shape.c).  Returns 0, or -1 on a malformed A or failed allocation. */
+int  orc_inverse_shape(int m, const DPlrMtx *A, DPlrMtx *B, double fill);
+
 /* Number of argument errors reported since load (the reference prints
  * them to stderr and returns without touching outputs). */
 long orc_error_count(void);

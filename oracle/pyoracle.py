@@ -49,6 +49,8 @@ def oracle(kind: str = "best") -> PlrApi:
         lib.orc_error_count.restype = ctypes.c_long
         lib.orc_set_threads.argtypes = [ctypes.c_int]
         lib.orc_blas_optimised.restype = ctypes.c_int
+        lib.orc_inverse_shape.restype = ctypes.c_int
+        lib.orc_inverse_shape.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]
         lib.orc_resid_dd.restype = ctypes.c_int
         lib.orc_resid_dd.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, c_double_p,
                                      ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,

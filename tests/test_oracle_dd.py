@@ -87,3 +87,27 @@ def test_dd_residual_rejects_bad_arguments():
                               x.ctypes.data_as(tree.c_double_p), 1)
     tree.free_c(a)
     assert rc == -1
+
+
+@pytest.mark.parametrize("seed", [0, 5])
+def test_inverse_shape_stand_in_has_the_inverse_ranks(seed):
+    """The timing stand-in for inv(A) (oracle/shape.c) has exactly the ranks
+    and stored entries of the inverse the oracle's dplrgeinv builds."""
+    orc = pyoracle.oracle("best")
+    t = gen.random_tree(1024, 32, [9, 0, 4, 7, 2], seed=seed)
+    a, binv, shape = tree.to_c(t), tree.new_empty(), tree.new_empty()
+    assert orc.geinv(t.size, a, binv, 0.0) == 0
+    assert orc.lib.orc_inverse_shape(t.size, a, shape, 0.5) == 0
+
+    def ranks(node, out):
+        if isinstance(node, tree.HNode):
+            out.append((node.ne.rank, node.sw.rank))
+            ranks(node.nw, out)
+            ranks(node.se, out)
+        return out
+
+    got, want = tree.from_c(shape), tree.from_c(binv)
+    assert ranks(got, []) == ranks(want, [])
+    assert orc.nz(t.size, shape) == orc.nz(t.size, binv)
+    for c in (a, binv, shape):
+        tree.free_c(c)
