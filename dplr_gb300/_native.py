@@ -94,6 +94,10 @@ def _bind(lib: ctypes.CDLL) -> None:
 # Entry points added by later modules of the library (bound when present).
 _OPTIONAL: list = [
     ("dplr_gpu_debug_fail_alloc", None, [c_int]),
+    ("dplr_gpu_debug_wait_limit", c_int, [c_int]),
+    ("dplr_gpu_plan_copy", c_int, [c_void_p, c_void_p, POINTER(c_void_p)]),
+    ("dplr_gpu_axpy", c_int, [c_double, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]),
+    ("dplr_gpu_gep2d", c_int, [c_void_p, c_void_p, c_longlong, c_void_p]),
 ]
 
 

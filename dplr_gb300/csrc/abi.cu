@@ -363,6 +363,8 @@ long long dplr_gpu_launch_count(void) { return dg::g_launches.load(); }
 
 void dplr_gpu_debug_fail_alloc(int after) { dg::g_fail_countdown.store(after < 0 ? -1 : after); }
 
+int dplr_gpu_debug_wait_limit(int spins) { return dg::set_wait_limit(spins); }
+
 int dplr_gpu_profile_start(void)
 {
     std::lock_guard<std::mutex> lk(dg::g_prof_mu);

@@ -27,63 +27,71 @@ constexpr int kSlab = 32;     // rows of X / factor staged per step
 constexpr int kRankTile = 64; // ranks handled per pass of the panel kernel
 
 // ----------------------------------------------------------------- panel
-// One CTA per (item, rhs tile).  Thread t owns rank column k = t % 64 of
-// the current rank tile and the rows i == t/64 (mod 4) of each slab; the
-// four row groups are summed through shared memory at the end.
+// One CTA per (item, rhs tile).  The rank tile RT (8, 16, 32 or 64 columns)
+// follows the item's rank, so blocks of small rank do not pay for 64
+// columns: thread t owns rank column k = t % RT and the rows t / RT (mod G),
+// G = 256 / RT, of each slab of 4 G rows; the G row groups are summed
+// through shared memory at the end.
 template <int NB>
 __global__ void __launch_bounds__(kThreads) panel_kernel(
     const PanelItem *__restrict__ items, const double *__restrict__ fbase,
     const double *__restrict__ X, int ldx, int nrhs, double *__restrict__ partials)
 {
-    constexpr int kStage = kSlab * (kRankTile + 1) + kSlab * NB;
-    constexpr int kRed = 4 * kRankTile * NB;
+    // staging: at most 4 G (RT + 1) <= 1152 factor doubles and 4 G NB <= 128 NB
+    // of X (RT = 8); the reduction: G RT NB = 256 NB
+    constexpr int kStage = 1152 + 128 * NB;
+    constexpr int kRed = kThreads * NB;
     __shared__ double sm[kStage > kRed ? kStage : kRed];
-    double(*Fs)[kRankTile + 1] = reinterpret_cast<double(*)[kRankTile + 1]>(sm);
-    double(*Xs)[NB] = reinterpret_cast<double(*)[NB]>(sm + kSlab * (kRankTile + 1));
-    double(*red)[kRankTile][NB] = reinterpret_cast<double(*)[kRankTile][NB]>(sm);
 
     const PanelItem it = items[blockIdx.x];
     const double *F = fbase + it.f;
     const int j0 = blockIdx.y * NB;
     const int nj = min(NB, nrhs - j0);
+    int RT = 8;
+    while (RT < it.rank && RT < kRankTile) RT <<= 1;
+    const int G = kThreads / RT, S = 4 * G;
+    double *Fs = sm;                     // S x (RT + 1)
+    double *Xs = sm + S * (RT + 1);      // S x NB
     const int t = threadIdx.x;
-    const int kk = t % kRankTile, g = t / kRankTile;
+    const int kk = t % RT, g = t / RT;
     double *P = partials + it.p * nrhs + (long long)it.chunk * it.rank * nrhs;
 
-    for (int kt = 0; kt < it.rank; kt += kRankTile) {
-        const int nk = min(kRankTile, it.rank - kt);
+    for (int kt = 0; kt < it.rank; kt += RT) {
+        const int nk = min(RT, it.rank - kt);
         double acc[NB];
 #pragma unroll
         for (int j = 0; j < NB; ++j) acc[j] = 0.0;
-        for (int s0 = 0; s0 < it.len; s0 += kSlab) {
-            const int ns = min(kSlab, it.len - s0);
+        for (int s0 = 0; s0 < it.len; s0 += S) {
+            const int ns = min(S, it.len - s0);
             __syncthreads();
-            for (int e = t; e < kSlab * kRankTile; e += kThreads) {
-                int r = e % kSlab, c = e / kSlab;
-                Fs[r][c] = (r < ns && c < nk) ? F[(long long)(kt + c) * it.n + it.r0 + s0 + r] : 0.0;
+            for (int e = t; e < S * RT; e += kThreads) {
+                int r = e % S, c = e / S;
+                Fs[r * (RT + 1) + c] = (r < ns && c < nk) ? F[(long long)(kt + c) * it.n + it.r0 + s0 + r] : 0.0;
             }
-            for (int e = t; e < kSlab * NB; e += kThreads) {
-                int r = e % kSlab, c = e / kSlab;
-                Xs[r][c] = (r < ns && c < nj)
-                               ? X[(long long)(j0 + c) * ldx + it.in0 + it.r0 + s0 + r]
-                               : 0.0;
+            for (int e = t; e < S * NB; e += kThreads) {
+                int r = e % S, c = e / S;
+                Xs[r * NB + c] = (r < ns && c < nj)
+                                     ? X[(long long)(j0 + c) * ldx + it.in0 + it.r0 + s0 + r]
+                                     : 0.0;
             }
             __syncthreads();
 #pragma unroll 4
-            for (int r = g; r < kSlab; r += 4) {
-                double f = Fs[r][kk];
+            for (int r = g; r < S; r += G) {
+                double f = Fs[r * (RT + 1) + kk];
 #pragma unroll
-                for (int j = 0; j < NB; ++j) acc[j] = fma(f, Xs[r][j], acc[j]);
+                for (int j = 0; j < NB; ++j) acc[j] = fma(f, Xs[r * NB + j], acc[j]);
             }
         }
-        __syncthreads();   // red aliases the staging buffers
+        __syncthreads();   // the reduction aliases the staging buffers
 #pragma unroll
-        for (int j = 0; j < NB; ++j) red[g][kk][j] = acc[j];
+        for (int j = 0; j < NB; ++j) sm[(g * RT + kk) * NB + j] = acc[j];
         __syncthreads();
-        if (g == 0 && kk < nk) {
-            for (int j = 0; j < nj; ++j) {
-                double s = red[0][kk][j] + red[1][kk][j] + red[2][kk][j] + red[3][kk][j];
-                P[(kt + kk) + (long long)(j0 + j) * it.rank] = s;
+        for (int e = t; e < RT * NB; e += kThreads) {
+            const int k2 = e % RT, j = e / RT;
+            if (k2 < nk && j < nj) {
+                double s = 0.0;
+                for (int gg = 0; gg < G; ++gg) s += sm[(gg * RT + k2) * NB + j];
+                P[(kt + k2) + (long long)(j0 + j) * it.rank] = s;
             }
         }
         __syncthreads();

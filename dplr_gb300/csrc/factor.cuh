@@ -51,5 +51,6 @@ int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double 
 long long factor_bytes(const Plan *p);
 int axpby_device(int m, int n, double a, const double *X, int ldx, double b, double *Y, int ldy,
                  cudaStream_t st);
+int refine_fixed(Plan *p, int n, const double *B, int ldb, double *X, int ldx, int corrections, cudaStream_t st);
 
 }  // namespace dg

@@ -231,6 +231,7 @@ int persist_apply(Plan *p, int trans, int nrhs, double alpha, const double *X, i
 // sliced.cu: the plan's mapped error flag of kernels with bounded waits
 int ensure_err_flag(Plan *p);
 int sliced_error(Plan *p);
+int set_wait_limit(int spins);
 
 // pairs.cu: FP64-accurate 1-RHS apply on the FP32 pipes
 int pairs_prepare(Plan *p, cudaStream_t st);

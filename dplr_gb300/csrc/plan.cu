@@ -371,6 +371,12 @@ int plan_build_forest(int count, const int *ms, const DPlrMtx *const *As, cudaSt
                     pool_bytes, cudaGetErrorString(e));
     }
     bytes += (long long)pool_bytes;
+    // the 256-byte alignment gaps between arrays are zero, so that two plans
+    // of equal factors have equal pools
+    if (cudaMemsetAsync(p->pool, 0, pool_bytes, st) != cudaSuccess) {
+        plan_free(p);
+        return fail(DPLR_GPU_ECUDA, "plan: cannot clear the factor pool");
+    }
     if ((rc = upload_vec(p->lr, &p->d_lr, &bytes)) || (rc = upload_vec(p->leaves, &p->d_leaves, &bytes)) ||
         (rc = upload_schedule(p->sched[0], &bytes)) || (rc = upload_schedule(p->sched[1], &bytes))) {
         plan_free(p);

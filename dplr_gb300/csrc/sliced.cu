@@ -712,6 +712,13 @@ int ensure_err_flag(Plan *p)
     return 0;
 }
 
+int set_wait_limit(int spins)
+{
+    const int v = spins > 0 ? spins : tc2::kSpin;
+    DG_CUDA(cudaMemcpyToSymbol(tc2::g_wait_limit, &v, sizeof(int)));
+    return 0;
+}
+
 int sliced_error(Plan *p)
 {
     if (!p->tc_err_h) return 0;

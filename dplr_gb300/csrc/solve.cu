@@ -63,6 +63,26 @@ int axpby_device(int m, int n, double a, const double *X, int ldx, double b, dou
     return 0;
 }
 
+// X := A^-1 B refined by `corrections` fixed FP64 steps (R = B - A X with
+// the FP64 apply, X += A^-1 R), with no host synchronisation, so that the
+// whole refined solve can be captured in a CUDA graph.  Scratch: p->ybuf
+// (2 m n doubles; sized by an ordinary call before any capture).
+int refine_fixed(Plan *p, int n, const double *B, int ldb, double *X, int ldx, int corrections, cudaStream_t st)
+{
+    const int m = p->m;
+    int rc = ensure_buffer(&p->ybuf, &p->ybuf_doubles, (size_t)2 * m * n);
+    if (rc) return rc;
+    double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
+    if ((rc = factor_solve(p, 0, n, B, ldb, X, ldx, st))) return rc;
+    for (int it = 0; it < corrections; ++it) {
+        if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
+        if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        if ((rc = factor_solve(p, 0, n, R, m, D, m, st))) return rc;
+        if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
+    }
+    return 0;
+}
+
 int colnorms_device(const double *A, int m, int n, int lda, double *out, cudaStream_t st)
 {
     if (n <= 0) return 0;

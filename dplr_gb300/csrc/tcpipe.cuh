@@ -52,6 +52,11 @@ constexpr int kSmem = 192 * 1024;
 constexpr int kColCap = 1024;          // right-hand sides whose output exponents the lean expand gathers
 constexpr int kNoExpT = -(1 << 24);    // "no entry" exponent (below every finite one)
 constexpr int kSpin = 1 << 22;
+// Bound of the role-to-role waits (wait_bar), read once per CTA at set-up.
+// dplr_gpu_debug_wait_limit lowers it so that a test can make the waits
+// expire and check the error path; the drain waits after an abort keep
+// kSpin, so copies and MMAs in flight always land before the CTA exits.
+__device__ int g_wait_limit = kSpin;
 
 template <int NS>
 struct Cfg {
@@ -217,6 +222,7 @@ struct Ctl {
     uint64_t full[8], empty[8];
     uint64_t accf, acce;
     uint32_t tmem;
+    int limit;
     volatile int abort;
 };
 
@@ -225,7 +231,7 @@ struct Ctl {
 __device__ __forceinline__ bool wait_bar(Ctl &c, uint64_t *bar, uint32_t parity)
 {
     const uint32_t a = su32(bar);
-    for (int it = 0; it < kSpin; ++it) {
+    for (int it = 0; it < c.limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -277,11 +283,46 @@ __device__ __forceinline__ void issue(uint32_t tmem, uint64_t ad0, uint64_t bd0,
     }
 }
 
+// The same products with 64-row B slices, one MMA per (A slice p, group of
+// up to four B slices q0..q0+k-1).  The B slices of a stage are contiguous
+// 64-row tile-blocks, so k of them form one operand of N = 64 k rows with
+// the same descriptor strides; its output columns j land on TMEM column
+// (p + q0 - 2) * 64 + j, which is diagonal d = p + q0 + j / 64, column
+// j % 64 -- exactly where the per-pair MMAs put them.  A slice p is read
+// from shared memory once per group instead of once per pair (12 MMAs of
+// N <= 256 instead of 36 of N = 64 for 8 slices), which takes the MMAs off
+// the shared-memory bound.  Needs D <= NS + 1: then every diagonal gets its
+// first pair from p = 1, so FIRST overwrites exactly at p == 1.
+template <int NS, int D, bool FIRST>
+__device__ __forceinline__ void issue_wide(uint32_t tmem, uint64_t ad0, uint64_t bd0, uint32_t bstep)
+{
+    static_assert(D <= NS + 1, "wide issue needs every diagonal to start at p = 1");
+#pragma unroll
+    for (int p = 1; p <= NS; ++p) {
+        const int qmax = D - p < NS ? D - p : NS;
+#pragma unroll
+        for (int q0 = 1; q0 <= qmax; q0 += 4) {
+            const int k = qmax - q0 + 1 < 4 ? qmax - q0 + 1 : 4;
+            mma_n(tmem + (uint32_t)((p + q0 - 2) * N), ad0 + (uint64_t)((p - 1) * (TB_A * 2 / 16)),
+                  bd0 + (uint64_t)(q0 - 1) * bstep, idesc_n(N * k), (FIRST && p == 1) ? 0u : 1u);
+        }
+    }
+}
+
 template <int NS, int D>
 __device__ __forceinline__ void issue_stage(uint32_t tmem, uint32_t a0, int nb, uint32_t idesc, bool first)
 {
     const uint64_t ad0 = sdesc(a0), bd0 = sdesc(a0 + NS * TB_A * 2);
     const uint32_t bstep = (uint32_t)(nb * KB * 2 / 16);
+    if constexpr (D <= NS + 1) {
+        if (nb == N) {
+            if (first)
+                issue_wide<NS, D, true>(tmem, ad0, bd0, bstep);
+            else
+                issue_wide<NS, D, false>(tmem, ad0, bd0, bstep);
+            return;
+        }
+    }
     if (first)
         issue<NS, D, true>(tmem, ad0, bd0, bstep, idesc);
     else
@@ -299,6 +340,7 @@ __device__ __forceinline__ void setup(Ctl &ctl, int warp, int lane)
         tc::mbar_init(&ctl.accf, 1);
         tc::mbar_init(&ctl.acce, EW);
         ctl.abort = 0;
+        ctl.limit = g_wait_limit;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {

@@ -120,6 +120,29 @@ class GpuPlan:
                       "dplr_gpu_adpy")
         self.factored = self.factored_transposed = self.sliced = self.mixed = False
 
+    def copy(self, stream=None) -> "GpuPlan":
+        """A new plan equal to this one, made on the device (dplrcpy)."""
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().dplr_gpu_plan_copy(self._h, _stream_ptr(stream), ctypes.byref(h)),
+                      "dplr_gpu_plan_copy")
+        return GpuPlan(None, _handle=h)
+
+    def axpy(self, alpha: float, other: "GpuPlan", stream=None) -> "GpuPlan":
+        """A new plan alpha * self + other, made on the device with dplraxpy's
+        layout (other's columns, then self's; ranks add)."""
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().dplr_gpu_axpy(float(alpha), self._h, other._h, _stream_ptr(stream),
+                                                  ctypes.byref(h)), "dplr_gpu_axpy")
+        return GpuPlan(None, _handle=h)
+
+    def to_dense(self, stream=None) -> torch.Tensor:
+        """The dense m x m matrix on the device (dplrgep2d), as a (m, m)
+        tensor whose row j is column j of the matrix."""
+        d = torch.empty(self.m, self.m, dtype=torch.float64, device="cuda")
+        _native.check(_native.lib().dplr_gpu_gep2d(self._h, d.data_ptr(), self.m, _stream_ptr(stream)),
+                      "dplr_gpu_gep2d")
+        return d
+
     def prepare_pairs(self, stream=None) -> None:
         """Float-pair copy of the factors: 1-RHS op-N applies then run on the
         FP32 pipes (FP64-accurate, compensated sums) at HBM speed."""

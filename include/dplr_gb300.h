@@ -79,6 +79,20 @@ DPLR_API int dplr_gpu_prepare_pairs(dplr_gpu_plan plan, void *stream);
 DPLR_API int dplr_gpu_scal(dplr_gpu_plan plan, double alpha, void *stream);
 DPLR_API int dplr_gpu_adpy(dplr_gpu_plan plan, double alpha, const double *D, void *stream);
 
+/* Structure arithmetic between device-resident plans (no host trees):
+ * dplr_gpu_plan_copy makes *out a new plan equal to `plan` (DPLR's dplrcpy,
+ * src/dplrcpy.c:19); dplr_gpu_axpy makes *out a new plan C = alpha A + B for
+ * plans of one structure, with DPLR's dplraxpy layout (src/dplraxpy.c:17-138:
+ * every low-rank block holds B's columns then A's, A's sig scaled by
+ * |alpha| and its u negated for alpha < 0, rank r_A + r_B; leaves B +
+ * alpha A; alpha == 0 gives a copy of B); dplr_gpu_gep2d writes the dense
+ * m x m matrix into the device array D (ld ldd, DPLR's dplrgep2d,
+ * src/dplrp2d.c:98; zero outside the trees of a batch).  New plans are not
+ * factored and hold no sliced copies. */
+DPLR_API int dplr_gpu_plan_copy(dplr_gpu_plan plan, void *stream, dplr_gpu_plan *out);
+DPLR_API int dplr_gpu_axpy(double alpha, dplr_gpu_plan A, dplr_gpu_plan B, void *stream, dplr_gpu_plan *out);
+DPLR_API int dplr_gpu_gep2d(dplr_gpu_plan plan, double *D, long long ldd, void *stream);
+
 /* Woodbury factorisation of the planned matrix (replaces forming inv(A)
  * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):
  * leaf inverses, per-level panels Z = D^-1 W and capacitance inverses
@@ -202,8 +216,12 @@ DPLR_API int dplr_gpu_batch_create(int count, const int *m, DPlrMtx *const *A, v
                                    dplr_gpu_plan *plan);
 DPLR_API int dplr_gpu_batch_offsets(dplr_gpu_plan plan, int *count, int *row0);
 
-/* CUDA graph of one apply (op 'A': Y = op(A) X) or one solve (op 'S':
- * Y = op(A)^-1 X, needs dplr_gpu_factor) with fixed device arrays: built
+/* CUDA graph of one apply (op 'A': Y = op(A) X), one solve (op 'S':
+ * Y = op(A)^-1 X, needs dplr_gpu_factor) or one solve refined by one FP64
+ * correction step (op 'R', trans 'N': Y = A^-1 X, R = X - A Y with the FP64
+ * apply, Y += A^-1 R; no host synchronisation inside, so the whole refined
+ * solve is one replay; dplr_gpu_residual checks the result) with fixed
+ * device arrays: built
  * once (one ordinary run sizes the scratch, a second run is captured on an
  * internal stream), then replayed by dplr_gpu_graph_launch on any stream
  * with one launch call.  Valid while the plan, its factorisation and the
@@ -237,6 +255,15 @@ DPLR_API long long dplr_gpu_launch_count(void);
  * drop-ins print their message) and leaves its outputs untouched.  No
  * counterpart in DPLR. */
 DPLR_API void dplr_gpu_debug_fail_alloc(int after);
+/* Fault injection for tests: the bound (in polls) of the waits between the
+ * roles of the tensor-core kernels, on the current device, for launches from
+ * now on; spins <= 0 restores the default (about 4 million polls).  With a
+ * bound of a few polls the waits expire: the kernel stops its work, lets the
+ * copies and MMAs in flight land, frees its tensor memory and records the
+ * expiry, which the plan's next call returns as DPLR_GPU_ECUDA ("a bounded
+ * wait expired"); the call after that runs normally.  No counterpart in
+ * DPLR. */
+DPLR_API int dplr_gpu_debug_wait_limit(int spins);
 DPLR_API int dplr_gpu_profile_start(void);
 DPLR_API int dplr_gpu_profile_stop(void);
 DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double *flops,

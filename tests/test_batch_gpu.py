@@ -82,7 +82,7 @@ def test_graph_replay_matches_direct_calls():
     S = torch.zeros_like(X)
     ga = GpuGraph(batch, "A", X, Y)
     gs = GpuGraph(batch, "S", X, S)
-    assert ga.kernels >= 3 and gs.kernels >= 3
+    assert ga.kernels >= 1 and gs.kernels >= 3        # the apply is one persistent launch
     for _ in range(3):
         Y.zero_()
         S.zero_()

