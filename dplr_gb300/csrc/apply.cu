@@ -289,26 +289,28 @@ __global__ void __launch_bounds__(kThreads) expand_kernel(
             B = X + tt.x_row0 + (long long)j0 * ldx;
             ldb = ldx;
         }
+        // K slabs of up to kSlab: only the nk live columns are staged and
+        // multiplied, so terms of small rank cost what they need
         for (int k0 = 0; k0 < tt.K; k0 += kSlab) {
             const int nk = min(kSlab, tt.K - k0);
             __syncthreads();
             if (!tt.trans_a) {
-                for (int e = t; e < R * kSlab; e += kThreads) {
+                for (int e = t; e < R * nk; e += kThreads) {
                     int r = e % R, c = e / R;
-                    As[r][c] = c < nk ? A[r + (long long)(k0 + c) * tt.lda] : 0.0;
+                    As[r][c] = A[r + (long long)(k0 + c) * tt.lda];
                 }
             } else {
-                for (int e = t; e < R * kSlab; e += kThreads) {
-                    int c = e % kSlab, r = e / kSlab;
-                    As[r][c] = c < nk ? A[(long long)r * tt.lda + k0 + c] : 0.0;
+                for (int e = t; e < R * nk; e += kThreads) {
+                    int c = e % nk, r = e / nk;
+                    As[r][c] = A[(long long)r * tt.lda + k0 + c];
                 }
             }
-            for (int e = t; e < kSlab * NB; e += kThreads) {
-                int r = e % kSlab, c = e / kSlab;
-                Bs[r][c] = (r < nk && c < nj) ? B[k0 + r + (long long)c * ldb] : 0.0;
+            for (int e = t; e < nk * NB; e += kThreads) {
+                int r = e % nk, c = e / nk;
+                Bs[r][c] = c < nj ? B[k0 + r + (long long)c * ldb] : 0.0;
             }
             __syncthreads();
-            for (int c = g; c < kSlab; c += G) {
+            for (int c = g; c < nk; c += G) {
                 double a = As[i][c];
 #pragma unroll
                 for (int j = 0; j < NB; ++j) acc[j] = fma(a, Bs[c][j], acc[j]);

@@ -29,7 +29,7 @@ struct GraphH {
 int run_op(Plan *p, char op, int trans, int n, const double *X, int ldx, double *Y, int ldy, cudaStream_t st)
 {
     if (op == 'A' || op == 'a') return apply_device(p, trans, n, 1.0, X, ldx, 0.0, Y, ldy, st, false);
-    if (op == 'R' || op == 'r') return refine_fixed(p, n, X, ldx, Y, ldy, 1, st);
+    if (op == 'R' || op == 'r') return refine_fixed(p, n, X, ldx, Y, ldy, 2, st);
     return factor_solve(p, trans, n, X, ldx, Y, ldy, st);
 }
 
@@ -83,7 +83,7 @@ int dplr_gpu_graph_create(dplr_gpu_plan plan, char op, char trans, int n, const 
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: invalid n, leading dimension or pointers");
     if (!(op == 'A' || op == 'a' || op == 'S' || op == 's' || op == 'R' || op == 'r'))
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: op must be 'A' (apply), 'S' (solve) or 'R' "
-                                     "(solve with one refinement step)");
+                                     "(solve with two refinement steps)");
     const int tr = !(trans == 'N' || trans == 'n');
     if ((op == 'R' || op == 'r') && tr)
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: the refined solve is op N only");

@@ -251,31 +251,32 @@ __device__ void expand_unit(const Args &a, int tile, int jt, double *sm)
         const double *B = fromT ? a.T + tt.b * a.nrhs + (long long)j0 * tt.ldb
                                 : a.X + tt.x_row0 + (long long)j0 * a.ldx;
         const long long ldb = fromT ? tt.ldb : a.ldx;
+        // only the nk live columns of a slab are staged and multiplied
         for (int k0 = 0; k0 < tt.K; k0 += kExpSlab) {
             const int nk = min(kExpSlab, tt.K - k0);
             __syncthreads();
             if (!tt.trans_a) {
-                for (int e = t; e < R * kExpSlab; e += kPT) {
+                for (int e = t; e < R * nk; e += kPT) {
                     const int r = e % R, c = e / R;
-                    As[r][c] = c < nk ? __ldg(A + r + (long long)(k0 + c) * tt.lda) : 0.0;
+                    As[r][c] = __ldg(A + r + (long long)(k0 + c) * tt.lda);
                 }
             } else {
-                for (int e = t; e < R * kExpSlab; e += kPT) {
-                    const int c = e % kExpSlab, r = e / kExpSlab;
-                    As[r][c] = c < nk ? __ldg(A + (long long)r * tt.lda + k0 + c) : 0.0;
+                for (int e = t; e < R * nk; e += kPT) {
+                    const int c = e % nk, r = e / nk;
+                    As[r][c] = __ldg(A + (long long)r * tt.lda + k0 + c);
                 }
             }
-            for (int e = t; e < kExpSlab * NB; e += kPT) {
-                const int r = e % kExpSlab, c = e / kExpSlab;
+            for (int e = t; e < nk * NB; e += kPT) {
+                const int r = e % nk, c = e / nk;
                 double v = 0.0;
-                if (r < nk && c < nj) {
+                if (c < nj) {
                     const double *src = B + k0 + r + (long long)c * ldb;
                     v = fromT ? __ldcg(src) : __ldg(src);
                 }
                 Bs[r][c] = v;
             }
             __syncthreads();
-            for (int c = g; c < kExpSlab; c += G) {
+            for (int c = g; c < nk; c += G) {
                 const double av = As[i][c];
 #pragma unroll
                 for (int j = 0; j < NB; ++j) acc[j] = fma(av, Bs[c][j], acc[j]);

@@ -1803,10 +1803,16 @@ long long layout_v(const Plan *p, std::vector<std::array<long long, 4>> &vdst, s
 }
 
 // Panel items of one block (row chunks of CH rows x rank tiles of 64).
+// Each (chunk, rank, right-hand side) leaves one 128-bit partial that the
+// reduce reads back: the residual's panel, which covers every level in one
+// launch and has work items to spare, takes chunks of kResidChunk rows
+// (4x fewer partials to write and read); the per-level panels of the inner
+// solve keep 1024-row chunks to spread one level over the SMs.
+constexpr int kInnerChunk = 1024, kResidChunk = 4096;
+
 void panel_items(const LRDesc &L, const std::array<long long, 4> &vdst, const std::array<int, 4> &vnr, long long poff,
-                 std::vector<PItem> &out)
+                 std::vector<PItem> &out, int CH = kInnerChunk)
 {
-    const int CH = 1024;
     const int nch = (L.n + CH - 1) / CH;
     for (int c = 0; c < nch; ++c) {
         const int r0 = c * CH, len = std::min(CH, L.n - r0);
@@ -2024,8 +2030,8 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     for (size_t b = 0; b < p->lr.size(); ++b) {
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
-        panel_items(L, vdst[b], vnr[b], poff, A.pitems);
-        const int nch = (L.n + 1023) / 1024;
+        panel_items(L, vdst[b], vnr[b], poff, A.pitems, kResidChunk);
+        const int nch = (L.n + kResidChunk - 1) / kResidChunk;
         const int nkb = (L.rank + 15) / 16;
         ridx[b] = (int)A.reduces.size();
         A.reduces.push_back(SReduceItem{poff, L.toff, -1, L.rank, nch, ev_off[b], nkb * 16, tpre});   // sig in V
@@ -2329,8 +2335,8 @@ static int mixed_build_tb_t(Plan *p, MixedSliced *M, Fact *F, cudaStream_t st)
         for (int b : F->lv[l].blocks) {
             const LRDesc &L = p->lr[b];
             if (L.rank == 0) continue;
-            panel_items(L, vdst[b], vnr[b], poff, S.pitems);
-            const int nch = (L.n + 1023) / 1024;
+            panel_items(L, vdst[b], vnr[b], poff, S.pitems, kInnerChunk);
+            const int nch = (L.n + kInnerChunk - 1) / kInnerChunk;
             const int ridx = (int)S.reduces.size();
             S.reduces.push_back(SReduceItem{poff, L.toff, -1, L.rank, nch, ev_off[b], pad16(L.rank), tpre[b]});   // sig in V
             poff += (long long)nch * L.rank;

@@ -63,10 +63,12 @@ int axpby_device(int m, int n, double a, const double *X, int ldx, double b, dou
     return 0;
 }
 
-// X := A^-1 B refined by `corrections` fixed FP64 steps (R = B - A X with
-// the FP64 apply, X += A^-1 R), with no host synchronisation, so that the
-// whole refined solve can be captured in a CUDA graph.  Scratch: p->ybuf
-// (2 m n doubles; sized by an ordinary call before any capture).
+// X := A^-1 B refined by `corrections` fixed steps (R = B - A X, X += A^-1 R
+// with the FP64 sweep), with no host synchronisation, so that the whole
+// refined solve can be captured in a CUDA graph.  The residual uses the
+// exact-slice products when the plan has them (dplr_gpu_prepare_sliced),
+// else the FP64 apply.  Scratch: p->ybuf (2 m n doubles) and the sliced
+// scratch, sized by an ordinary call before any capture.
 int refine_fixed(Plan *p, int n, const double *B, int ldb, double *X, int ldx, int corrections, cudaStream_t st)
 {
     const int m = p->m;
@@ -75,8 +77,12 @@ int refine_fixed(Plan *p, int n, const double *B, int ldb, double *X, int ldx, i
     double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
     if ((rc = factor_solve(p, 0, n, B, ldb, X, ldx, st))) return rc;
     for (int it = 0; it < corrections; ++it) {
-        if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
-        if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        if (p->sliced) {
+            if ((rc = sliced_residual(p, n, X, ldx, B, ldb, R, m, st))) return rc;
+        } else {
+            if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
+            if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        }
         if ((rc = factor_solve(p, 0, n, R, m, D, m, st))) return rc;
         if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
     }

@@ -213,8 +213,9 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
         X[:k, o:o + t.size] = torch.randn(k, t.size, generator=g, dtype=torch.float64, device="cuda")
     Y = torch.empty_like(X)
     Z = torch.empty_like(X)
+    plan.prepare_sliced()                         # exact-slice residual of the correction step
     ga = GpuGraph(plan, "A", X, Y)
-    gs = GpuGraph(plan, "R", X, Z)                # solve + one FP64 correction, one replay
+    gs = GpuGraph(plan, "R", X, Z)                # solve + two corrections, one replay
     stream = torch.cuda.current_stream()
     for _ in range(max(3, warmup)):
         ga.launch()
@@ -241,8 +242,9 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
     flops = sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_s.values())
     fp64 = fp64_gemm_peak()
     tflops = flops / (ms / 1e3) / 1e12
-    # accuracy: every matrix's own right-hand sides, FP64 residual of the replayed refined solve
-    R = plan.residual(Z, X, precise=False)
+    # accuracy: every matrix's own right-hand sides, exact-slice residual of
+    # the replayed refined solve
+    R = plan.residual(Z, X, precise=True)
     worst = 0.0
     for o, t, k in zip(offs, trees, nrhs):
         rn = R[:k, o:o + t.size].norm(dim=1)
@@ -259,7 +261,7 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
                      "algorithmic": f"{flops:.4g} flop per step (sum of the launches' algorithmic counts, "
                                     f"stacked right-hand sides)"},
         "config": {"workload": "512 1D exponential-kernel PLR matrices, N in [1024, 16384], leaf 64, "
-                               "ranks 1-4, 1-16 RHS each; one apply graph + one refined-solve graph per step",
+                               "ranks 1-4, 1-16 RHS each; one apply graph + one refined-solve graph (two corrections) per step",
                    "matrices": count, "rows_total": plan.m, "rhs_total": total_rhs, "rhs_stacked": n,
                    "graph_kernels": {"apply": ga.kernels, "refined_solve": gs.kernels},
                    "autotune": tune, "refined_solve_max_rel_resid": worst,
@@ -269,12 +271,12 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
 
 
 def _refined_once(plan, b, x):
-    """Solve + one FP64 correction launch by launch (what the 'R' graph
+    """Solve + two corrections launch by launch (what the 'R' graph
     replays), for profiling."""
     x0 = plan.solve(b, out=x)
-    r = plan.residual(x0, b, precise=False)
-    d = plan.solve(r)
-    x0 += d
+    for _ in range(2):
+        r = plan.residual(x0, b, precise=plan.sliced)
+        x0 += plan.solve(r)
     return x0
 
 

@@ -217,8 +217,9 @@ DPLR_API int dplr_gpu_batch_create(int count, const int *m, DPlrMtx *const *A, v
 DPLR_API int dplr_gpu_batch_offsets(dplr_gpu_plan plan, int *count, int *row0);
 
 /* CUDA graph of one apply (op 'A': Y = op(A) X), one solve (op 'S':
- * Y = op(A)^-1 X, needs dplr_gpu_factor) or one solve refined by one FP64
- * correction step (op 'R', trans 'N': Y = A^-1 X, R = X - A Y with the FP64
+ * Y = op(A)^-1 X, needs dplr_gpu_factor) or one solve refined by two
+ * correction steps (op 'R', trans 'N': Y = A^-1 X, twice R = X - A Y with the
+ * exact-slice products if dplr_gpu_prepare_sliced was called, else the FP64
  * apply, Y += A^-1 R; no host synchronisation inside, so the whole refined
  * solve is one replay; dplr_gpu_residual checks the result) with fixed
  * device arrays: built
