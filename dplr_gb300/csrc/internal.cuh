@@ -184,6 +184,11 @@ struct Plan {
     int *tc_err_h = nullptr, *tc_err_d = nullptr;
     // float-pair copy of the factors for the 1-RHS apply (pairs.cu)
     void *pairs = nullptr;
+    // host <-> device copies of the refined host solve split over streams
+    // (one copy engine each), created on first use (solve.cu)
+    static constexpr int kCopyStreams = 4;
+    cudaStream_t copy_st[kCopyStreams] = {};
+    cudaEvent_t copy_ev[kCopyStreams + 1] = {};
     // factor gradients (grad.cu): work lists and scratch
     void *grad = nullptr;
     double *gbuf = nullptr;

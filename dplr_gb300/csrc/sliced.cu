@@ -1804,11 +1804,10 @@ long long layout_v(const Plan *p, std::vector<std::array<long long, 4>> &vdst, s
 
 // Panel items of one block (row chunks of CH rows x rank tiles of 64).
 // Each (chunk, rank, right-hand side) leaves one 128-bit partial that the
-// reduce reads back: the residual's panel, which covers every level in one
-// launch and has work items to spare, takes chunks of kResidChunk rows
-// (4x fewer partials to write and read); the per-level panels of the inner
-// solve keep 1024-row chunks to spread one level over the SMs.
-constexpr int kInnerChunk = 1024, kResidChunk = 4096;
+// reduce reads back.  Measured on the N = 2^18 solve, 4096-row chunks for
+// the residual's all-level panel cut the reduce (1.55 -> 1.40 ms per step)
+// but slowed the panel more (8.40 -> 9.17 ms): both panels keep 1024 rows.
+constexpr int kInnerChunk = 1024, kResidChunk = 1024;
 
 void panel_items(const LRDesc &L, const std::array<long long, 4> &vdst, const std::array<int, 4> &vnr, long long poff,
                  std::vector<PItem> &out, int CH = kInnerChunk)
