@@ -1633,31 +1633,69 @@ __device__ __forceinline__ void store8(long long (&v)[8], bf16 *out, long long s
     }
 }
 
-// X (m x nrhs) into 16-row x 64-column tile-blocks; one thread per
-// (column j, 8-row half h of row-block rb), j fastest, all 8 loads issued
-// before any use; columns >= nrhs are zero.
+// Four consecutive values of one column as NS bf16 digit slices: 8 bytes per
+// slice at out + p * stride (the same balanced base-128 split as store8).
 template <int NS>
-__global__ void xslice_tb_kernel(const double *__restrict__ X, int m, int ldx, int nrhs, int xnjt,
-                                 const int *__restrict__ xexp, bf16 *__restrict__ xs, long long stride)
+__device__ __forceinline__ void store4(long long (&v)[4], bf16 *out, long long stride)
 {
-    const int nrb = m >> 4, ncol = xnjt * 64;
-    const long long cnt = (long long)nrb * 2 * ncol;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(t % ncol);
-        const long long q = t / ncol;
-        const int h = (int)(q & 1), rb = (int)(q >> 1);
+#pragma unroll
+    for (int p = NS - 1; p >= 0; --p) {
+        uint32_t b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int a;
+            if (p > 0) {
+                const long long d = ((v[u] + 64) & 127) - 64;
+                a = (int)d;
+                v[u] = (v[u] - d) >> 7;
+            } else {
+                a = (int)v[u];
+            }
+            b[u] = digit_bits(a);
+        }
+        uint2 w;
+        w.x = b[0] | (b[1] << 16);
+        w.y = b[2] | (b[3] << 16);
+        *reinterpret_cast<uint2 *>(out + p * stride) = w;
+    }
+}
+
+// X (m x nrhs) into 16-row x 64-column tile-blocks, coalesced: one warp per
+// (row-block rb, group of 8 columns); lane l holds column 8 g + l / 4 and
+// rows 4 (l % 4) .. 4 (l % 4) + 3 of the row-block, so four lanes read one
+// column's 128 contiguous bytes and the warp writes, per slice, the 256
+// contiguous bytes of two core matrices.  Columns >= nrhs are zero.
+template <int NS>
+__global__ void xslice_tb4_kernel(const double *__restrict__ X, int m, int ldx, int nrhs, int xnjt,
+                                  const int *__restrict__ xexp, bf16 *__restrict__ xs, long long stride)
+{
+    const int nrb = m >> 4, ncg = xnjt * 8;
+    const long long nw = (long long)nrb * ncg;
+    const int lane = threadIdx.x & 31;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long wstep = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int q = lane & 3;
+    const bool vec = (ldx & 1) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+    for (long long w = w0; w < nw; w += wstep) {
+        const int g = (int)(w % ncg), rb = (int)(w / ncg);
+        const int j = g * 8 + (lane >> 2);
         const bool live = j < nrhs;
         const int sh = live ? 7 * NS - xexp[j] : 0;
-        const double *col = X + (long long)(live ? j : 0) * ldx + rb * 16 + h * 8;
-        bf16 *out = xs + ((long long)rb * xnjt + (j >> 6)) * kTbB + tc2::tbo(j & 63, 0) + h * 64;
-        double x[8];
+        const double *col = X + (long long)(live ? j : 0) * ldx + rb * 16 + q * 4;
+        double x[4];
+        if (live && vec) {
+            const double2 a = __ldg(reinterpret_cast<const double2 *>(col));
+            const double2 b = __ldg(reinterpret_cast<const double2 *>(col + 2));
+            x[0] = a.x, x[1] = a.y, x[2] = b.x, x[3] = b.y;
+        } else {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) x[u] = live ? col[u] : 0.0;
-        long long y[8];
+            for (int u = 0; u < 4; ++u) x[u] = live ? __ldg(col + u) : 0.0;
+        }
+        long long y[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) y[u] = scaled_int(x[u], sh);
-        store8<NS>(y, out, stride);
+        for (int u = 0; u < 4; ++u) y[u] = scaled_int(x[u], sh);
+        bf16 *out = xs + ((long long)rb * xnjt + (j >> 6)) * kTbB + tc2::tbo(j & 63, q * 4);
+        store4<NS>(y, out, stride);
     }
 }
 
@@ -1863,9 +1901,9 @@ int slice_x_tb(const double *X, int m, int ldx, int nrhs, bf16 *&xs, size_t &xs_
     } else {
         xcol_exps(X, m, ldx, nrhs, xexp, st);
     }
-    const long long cnt = (long long)(m / 16) * 2 * xnjt * 64;
-    const int grid = (int)std::min<long long>((cnt + 255) / 256, 152LL * 32);
-    xslice_tb_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
+    const long long warps = (long long)(m / 16) * xnjt * 8;
+    const int grid = (int)std::min<long long>((warps * 32 + 255) / 256, 152LL * 32);
+    xslice_tb4_kernel<NS><<<grid, 256, 0, st>>>(X, m, ldx, nrhs, xnjt, xexp, xs, (long long)(m / 16) * xnjt * kTbB);
     note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
