@@ -333,6 +333,20 @@ cudaError_t dev_malloc(void **ptr, size_t bytes)
     return cudaMalloc(ptr, bytes);
 }
 
+// Recompression after the operations that grow ranks (off unless a caller
+// sets a threshold with dplr_gpu_set_recompress).
+static std::atomic<double> g_recompress_eps{-1.0};
+
+double recompress_eps() { return g_recompress_eps.load(); }
+
+void recompress_after(int m, DPlrMtx *A)
+{
+    const double e = g_recompress_eps.load();
+    if (!(e >= 0.0) || !A) return;
+    if (dplr_gpu_reduce_svd(m, A, e, 0) != DPLR_GPU_OK)
+        fprintf(stderr, "dplr_gpu_reduce_svd: %s\n", last_error_c());
+}
+
 NvtxRange::NvtxRange(const char *name) { nvtxRangePushA(name); }
 NvtxRange::~NvtxRange() { nvtxRangePop(); }
 
@@ -364,6 +378,8 @@ long long dplr_gpu_launch_count(void) { return dg::g_launches.load(); }
 void dplr_gpu_debug_fail_alloc(int after) { dg::g_fail_countdown.store(after < 0 ? -1 : after); }
 
 int dplr_gpu_debug_wait_limit(int spins) { return dg::set_wait_limit(spins); }
+
+void dplr_gpu_set_recompress(double eps) { dg::g_recompress_eps.store(eps >= 0.0 ? eps : -1.0); }
 
 int dplr_gpu_profile_start(void)
 {

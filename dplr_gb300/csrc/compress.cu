@@ -37,6 +37,7 @@
 #include "../../include/dplr.h"
 #include "../../include/dplr_gb300.h"
 #include "gemm.cuh"
+#include "svdblock.cuh"
 
 namespace dg {
 int fail(int code, const char *fmt, ...);
@@ -418,11 +419,6 @@ __global__ void scale_cols_kernel(double *__restrict__ u, const double *__restri
         u[e] *= s[e / n];
 }
 
-// One low-rank block to recompress: its host node and threshold.
-struct RJob {
-    DPlrMtx *L;
-    double eps;
-};
 
 // Buffers of one recompression worker, sized for the largest block.
 struct RWorker {
@@ -502,17 +498,18 @@ struct RWorker {
 
     // U diag(s) V^T (n x n, rank r) -> its SVD truncated where sigma < eps:
     // QR of U diag(s) and of V, SVD of Ru Rv^T (k x k, k = min(n, r)).
+    // Sources and destinations may be host or device memory (UVA copies).
     // 0 done, 1 the SVD did not converge (block left as it was), -1 error.
-    int run(RJob &jb)
+    int run(dg::SvdBlock &jb)
     {
-        DPlrMtx *L = jb.L;
-        const int n = L->size, r = L->dlr.rank;
+        const int n = jb.n, r = jb.r;
+        jb.rank = r;
         if (r == 0 || n == 0) return 0;
         const int k = std::min(n, r);
         const size_t nr = (size_t)n * r;
-        if (cudaMemcpyAsync(U, L->dlr.u, nr * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(V, L->dlr.v, nr * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(sg, L->dlr.sig, (size_t)r * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        if (cudaMemcpyAsync(U, jb.u, nr * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess ||
+            cudaMemcpyAsync(V, jb.v, nr * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess ||
+            cudaMemcpyAsync(sg, jb.sig, (size_t)r * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
             return -1;
         scale_cols_kernel<<<128, 256, 0, st>>>(U, sg, n, r);
         dg::note_launch();
@@ -544,30 +541,81 @@ struct RWorker {
             if (!gemm({U, Um, nullptr, nullptr, Un, n, rank, k, n, k, 0, n, 0, 0, 1.0, 0.0}) ||
                 !gemm({V, Vmt, nullptr, nullptr, Vn, n, rank, k, n, k, 0, n, 0, 1, 1.0, 0.0}))
                 return -1;
-            if (cudaMemcpyAsync(L->dlr.u, Un, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-                    cudaSuccess ||
-                cudaMemcpyAsync(L->dlr.v, Vn, (size_t)n * rank * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+            if (cudaMemcpyAsync(jb.du, Un, (size_t)n * rank * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess ||
+                cudaMemcpyAsync(jb.dv, Vn, (size_t)n * rank * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess ||
+                cudaMemcpyAsync(jb.dsig, hS.data(), (size_t)rank * sizeof(double), cudaMemcpyDefault, st) !=
                     cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess)
                 return -1;
-            memcpy(L->dlr.sig, hS.data(), (size_t)rank * sizeof(double));
         }
-        L->dlr.rank = rank;
+        jb.rank = rank;
         return 0;
     }
 };
 
-void collect_rjobs(DPlrMtx *A, double eps, std::vector<RJob> &jobs)
+// Blocks of a host tree with dplrreduce's thresholds (eps/4 per level,
+// src/dplrreduce.c:46); `nodes` keeps each block's node for its new rank.
+void collect_rjobs(DPlrMtx *A, double eps, std::vector<dg::SvdBlock> &jobs, std::vector<DPlrMtx *> &nodes)
 {
     if (A->type != PLR_HMTX) return;
     const double e2 = eps / 4.0;
-    jobs.push_back({A->dh.ne, e2});
-    jobs.push_back({A->dh.sw, e2});
-    collect_rjobs(A->dh.nw, e2, jobs);
-    collect_rjobs(A->dh.se, e2, jobs);
+    for (DPlrMtx *L : {A->dh.ne, A->dh.sw}) {
+        jobs.push_back({L->dlr.u, L->dlr.v, L->dlr.sig, L->dlr.u, L->dlr.v, L->dlr.sig, L->size, L->dlr.rank, e2,
+                        L->dlr.rank});
+        nodes.push_back(L);
+    }
+    collect_rjobs(A->dh.nw, e2, jobs, nodes);
+    collect_rjobs(A->dh.se, e2, jobs, nodes);
 }
 
 }  // namespace
+
+namespace dg {
+
+int svd_truncate_blocks(SvdBlock *blocks, int count, int workers)
+{
+    int nmax = 0, rmax = 0;
+    for (int i = 0; i < count; ++i)
+        if (blocks[i].r > 0) {
+            nmax = std::max(nmax, blocks[i].n);
+            rmax = std::max(rmax, blocks[i].r);
+        }
+    if (rmax == 0) {
+        for (int i = 0; i < count; ++i) blocks[i].rank = blocks[i].r;
+        return 0;
+    }
+    if (!solver().ok) return report(DPLR_GPU_ECUDA, "SVD recompression: cannot load cuSOLVER (libcusolver.so.12)");
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long long)blocks[a].n * blocks[a].r > (long long)blocks[b].n * blocks[b].r;
+    });
+    int nw = workers > 0 ? workers : 8;
+    nw = std::max(1, std::min(nw, count));
+    std::vector<RWorker> pool(nw);
+    bool ok = true;
+    for (RWorker &w : pool) ok = ok && w.init(nmax, rmax);
+    std::vector<int> res(count, 0);
+    if (ok) {
+        std::atomic<int> next{0};
+        auto body = [&](RWorker &w) {
+            for (int k = next.fetch_add(1); k < count; k = next.fetch_add(1)) res[order[k]] = w.run(blocks[order[k]]);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nw; ++t) th.emplace_back(body, std::ref(pool[t]));
+        body(pool[0]);
+        for (std::thread &t : th) t.join();
+    }
+    for (RWorker &w : pool) w.release();
+    if (!ok) return report(DPLR_GPU_ECUDA, "SVD recompression: device setup failed");
+    for (int r : res)
+        if (r < 0) return report(DPLR_GPU_ECUDA, "SVD recompression: CUDA or cuSOLVER call failed");
+    for (int r : res)
+        if (r > 0) return report(DPLR_GPU_ENOTCONV, "SVD recompression: an SVD did not converge (block kept)");
+    return 0;
+}
+
+}  // namespace dg
 
 extern "C" {
 
@@ -678,42 +726,13 @@ int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers)
     if (!(eps >= 0.0)) return dg::fail(DPLR_GPU_EINVAL, "%s: eps must be nonnegative", fn);
     int rc = dg::validate_tree(m, A, fn);
     if (rc) return rc;
-    std::vector<RJob> jobs;
-    collect_rjobs(A, eps, jobs);
-    int nmax = 0, rmax = 0;
-    for (const RJob &j : jobs)
-        if (j.L->dlr.rank > 0) {
-            nmax = std::max(nmax, j.L->size);
-            rmax = std::max(rmax, j.L->dlr.rank);
-        }
-    if (rmax == 0) return 0;
-    if (!solver().ok) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: cannot load cuSOLVER (libcusolver.so.12)");
-    std::stable_sort(jobs.begin(), jobs.end(), [](const RJob &a, const RJob &b) {
-        return (long long)a.L->size * a.L->dlr.rank > (long long)b.L->size * b.L->dlr.rank;
-    });
-    int nw = workers > 0 ? workers : 8;
-    nw = std::max(1, std::min<int>(nw, (int)jobs.size()));
-    std::vector<RWorker> pool(nw);
-    bool ok = true;
-    for (RWorker &w : pool) ok = ok && w.init(nmax, rmax);
-    std::vector<int> res(jobs.size(), 0);
-    if (ok) {
-        std::atomic<int> next{0};
-        auto body = [&](RWorker &w) {
-            for (int k = next.fetch_add(1); k < (int)jobs.size(); k = next.fetch_add(1)) res[k] = w.run(jobs[k]);
-        };
-        std::vector<std::thread> th;
-        for (int t = 1; t < nw; ++t) th.emplace_back(body, std::ref(pool[t]));
-        body(pool[0]);
-        for (std::thread &t : th) t.join();
-    }
-    for (RWorker &w : pool) w.release();
-    if (!ok) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: device setup failed");
-    for (int r : res) {
-        if (r < 0) return report(DPLR_GPU_ECUDA, "dplr_gpu_reduce_svd: CUDA or cuSOLVER call failed");
-        if (r > 0) return report(DPLR_GPU_ENOTCONV, "dplr_gpu_reduce_svd: an SVD did not converge (block kept)");
-    }
-    return 0;
+    std::vector<dg::SvdBlock> jobs;
+    std::vector<DPlrMtx *> nodes;
+    collect_rjobs(A, eps, jobs, nodes);
+    rc = dg::svd_truncate_blocks(jobs.data(), (int)jobs.size(), workers);
+    // ranks only shrink; a block whose SVD failed keeps its rank
+    for (size_t i = 0; i < jobs.size(); ++i) nodes[i]->dlr.rank = jobs[i].rank;
+    return rc;
 }
 
 void dplrd2gep(int m, double *A, int lda, DPlrMtx *B, double eps, int nlvl, int *info)

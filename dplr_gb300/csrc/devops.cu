@@ -10,6 +10,7 @@
 // copy launch.  Low-rank columns are kept in DPLR's order: B's first, then
 // A's.
 #include "internal.cuh"
+#include "svdblock.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -204,6 +205,65 @@ __global__ void gep2d_kernel(const DenseTile *__restrict__ tiles, const LRDesc *
     }
 }
 
+// SVD recompression of every low-rank block of a plan into a new plan
+// (dplrreduce's thresholds: eps / 4^(depth + 1), src/dplrreduce.c:46): the
+// factors are read from the pool, each block's truncated SVD is written into
+// a scratch copy of the pool at the block's own offsets (ranks only
+// shrink), then the new plan with the new ranks is filled from it.
+int plan_reduce(Plan *p, double eps, int workers, cudaStream_t st, Plan **out)
+{
+    *out = nullptr;
+    DG_CUDA(cudaStreamSynchronize(st));       // the workers read the pool on their own streams
+    const size_t bytes = (size_t)std::max<long long>(p->pool_doubles, 1) * sizeof(double);
+    double *scratch = nullptr;
+    DG_ALLOC(&scratch, bytes);
+    // a block whose SVD does not converge keeps its factors: start from a copy
+    cudaError_t e = cudaMemcpy(scratch, p->pool, bytes, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(scratch);
+        return fail(DPLR_GPU_ECUDA, "plan recompression: %s", cudaGetErrorString(e));
+    }
+    std::vector<SvdBlock> blocks;
+    for (const LRDesc &L : p->lr) {
+        double thr = eps;
+        for (int l = 0; l <= L.level; ++l) thr /= 4.0;
+        blocks.push_back({p->pool + L.u, p->pool + L.v, p->pool + L.sig, scratch + L.u, scratch + L.v,
+                          scratch + L.sig, L.n, L.rank, thr, L.rank});
+    }
+    int rc = svd_truncate_blocks(blocks.data(), (int)blocks.size(), workers);
+    if (rc && rc != DPLR_GPU_ENOTCONV) {
+        cudaFree(scratch);
+        return rc;
+    }
+    std::vector<int> ranks;
+    for (const SvdBlock &b : blocks) ranks.push_back(b.rank);
+    Plan *c = nullptr;
+    int rc2 = clone_layout(p, ranks, &c);
+    if (rc2) {
+        cudaFree(scratch);
+        return rc2;
+    }
+    std::vector<CopyJob> jobs;
+    for (size_t i = 0; i < c->lr.size(); ++i) {
+        const LRDesc &dc = c->lr[i], &ds = p->lr[i];
+        const long long n = (long long)dc.n * dc.rank;
+        add_job(jobs, c->pool + dc.u, scratch + ds.u, nullptr, n, 1.0);
+        add_job(jobs, c->pool + dc.v, scratch + ds.v, nullptr, n, 1.0);
+        add_job(jobs, c->pool + dc.sig, scratch + ds.sig, nullptr, dc.rank, 1.0);
+    }
+    for (size_t i = 0; i < c->leaves.size(); ++i)
+        add_job(jobs, c->pool + c->leaves[i].d, p->pool + p->leaves[i].d, nullptr,
+                (long long)c->leaves[i].b * c->leaves[i].b, 1.0);
+    rc2 = run_jobs(jobs, st);
+    cudaFree(scratch);
+    if (rc2) {
+        plan_free(c);
+        return rc2;
+    }
+    *out = c;
+    return rc;        // DPLR_GPU_ENOTCONV reports the kept blocks, the plan is valid
+}
+
 }  // namespace
 
 }  // namespace dg
@@ -275,8 +335,30 @@ int dplr_gpu_axpy(double alpha, dplr_gpu_plan A, dplr_gpu_plan B, void *stream, 
         plan_free(c);
         return rc;
     }
+    // the ranks grew: recompress when dplr_gpu_set_recompress asked for it
+    const double reps = recompress_eps();
+    if (add && reps >= 0.0) {
+        Plan *r = nullptr;
+        rc = plan_reduce(c, reps, 0, (cudaStream_t)stream, &r);
+        plan_free(c);
+        if (!r) return rc;
+        c = r;
+    }
     *out = (dplr_gpu_plan)c;
     return 0;
+}
+
+int dplr_gpu_plan_reduce_svd(dplr_gpu_plan plan, double eps, int workers, void *stream, dplr_gpu_plan *out)
+{
+    dg::NvtxRange nvtx_("dplr_gpu_plan_reduce_svd");
+    Plan *p = (Plan *)plan;
+    if (!p || !out) return fail(DPLR_GPU_EINVAL, "dplr_gpu_plan_reduce_svd: null argument");
+    *out = nullptr;
+    if (!(eps >= 0.0)) return fail(DPLR_GPU_EINVAL, "dplr_gpu_plan_reduce_svd: eps must be nonnegative");
+    Plan *r = nullptr;
+    const int rc = plan_reduce(p, eps, workers, (cudaStream_t)stream, &r);
+    *out = (dplr_gpu_plan)r;
+    return rc;
 }
 
 int dplr_gpu_gep2d(dplr_gpu_plan plan, double *D, long long ldd, void *stream)

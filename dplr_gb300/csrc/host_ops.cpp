@@ -15,6 +15,10 @@
 
 #include "../../include/dplr.h"
 
+namespace dg {
+void recompress_after(int m, DPlrMtx *A);
+}
+
 extern "C" {
 
 void dplrscal(int m, double *alpha, DPlrMtx *A)
@@ -124,35 +128,45 @@ static void lr_axpy(int m, double alpha, DPlrMtx *A, DPlrMtx *B)
     B->dlr.rank = ra + rb;
 }
 
+static int axpy_tree(int m, double *alpha, DPlrMtx *A, DPlrMtx *B);
+
 void dplraxpy(int m, double *alpha, DPlrMtx *A, DPlrMtx *B)
+{
+    // recompress only a B that was added to, and only when
+    // dplr_gpu_set_recompress asked for it
+    if (axpy_tree(m, alpha, A, B) == 0 && *alpha != 0.0) dg::recompress_after(m, B);
+}
+
+static int axpy_tree(int m, double *alpha, DPlrMtx *A, DPlrMtx *B)
 {
     if (m < 0) {
         fprintf(stderr, "dplraxpy: invalid matrix size %d\n", m);
-        return;
+        return -1;
     }
     if (A->size != m || B->size != m) {
         fprintf(stderr, "dplraxpy: invalid A or B size\n");
-        return;
+        return -1;
     }
     if (A->type != B->type) {
         fprintf(stderr, "dplraxpy: A and B types do not match\n");
-        return;
+        return -1;
     }
     if (A->type != PLR_DMTX && A->type != PLR_HMTX) {
         fprintf(stderr, "dplraxpy: invalid A or B type\n");
-        return;
+        return -1;
     }
     const double a = *alpha;
-    if (a == 0.0) return;
+    if (a == 0.0) return 0;
     if (A->type == PLR_DMTX) {
         const size_t n = (size_t)m * m;
         for (size_t i = 0; i < n; ++i) B->dd.d[i] += a * A->dd.d[i];
-        return;
+        return 0;
     }
     lr_axpy(m / 2, a, A->dh.ne, B->dh.ne);
     lr_axpy(m / 2, a, A->dh.sw, B->dh.sw);
-    dplraxpy(m / 2, alpha, A->dh.nw, B->dh.nw);
-    dplraxpy(m / 2, alpha, A->dh.se, B->dh.se);
+    axpy_tree(m / 2, alpha, A->dh.nw, B->dh.nw);
+    axpy_tree(m / 2, alpha, A->dh.se, B->dh.se);
+    return 0;
 }
 
 void dplradpy(int m, double *alpha, double *D, DPlrMtx *B)

@@ -47,6 +47,12 @@ cudaError_t dev_malloc(void **ptr, size_t bytes);
                               __LINE__);                                                        \
     } while (0)
 
+// Recompression after rank-growing operations (dplr_gpu_set_recompress):
+// the threshold (< 0: off) and the host-tree hook the drop-ins call on their
+// output (dplr_gpu_reduce_svd with that threshold).
+double recompress_eps();
+void recompress_after(int m, DPlrMtx *A);
+
 // NVTX range around an entry point (visible in Nsight tools; a no-op unless
 // a tool is attached).
 struct NvtxRange {

@@ -587,6 +587,7 @@ extern "C" void dplrgeinv(int m, DPlrMtx *A, DPlrMtx *B, double eps, int *info)
     rp.appends();
     plan_free(p);
     *info = 0;
+    recompress_after(m, B);
 }
 
 // ---------------------------------------------------------------- geprk
@@ -792,4 +793,5 @@ extern "C" void dplrgeprk(int m, int k, double *alpha, double *u, int ldu, doubl
     } w{p, k, boff, hu, hv, hsig, hl, ljobs};
     w.go(A);
     plan_free(p);
+    recompress_after(m, A);
 }

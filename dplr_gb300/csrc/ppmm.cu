@@ -709,7 +709,9 @@ int dplr_gpu_geppmm(char transa, char transb, int m, double alpha, DPlrMtx *A, D
     if ((rc = validate_tree(m, A, fn)) || (rc = validate_tree(m, B, fn)) || (rc = validate_tree(m, C, fn))) return rc;
     if ((rc = same_structure(A, B, C, fn))) return rc;
     if (m == 0) return 0;
-    return geppmm_device(ta, tb, m, alpha, A, B, beta, C, eps, (cudaStream_t)stream);
+    rc = geppmm_device(ta, tb, m, alpha, A, B, beta, C, eps, (cudaStream_t)stream);
+    if (rc == 0) recompress_after(m, C);
+    return rc;
 }
 
 void dplr_gpu_release_staging(void)

@@ -135,6 +135,16 @@ class GpuPlan:
                                                   ctypes.byref(h)), "dplr_gpu_axpy")
         return GpuPlan(None, _handle=h)
 
+    def reduce_svd(self, eps: float, workers: int = 0, stream=None) -> "GpuPlan":
+        """A new plan with every low-rank block replaced by its truncated SVD
+        (dplrreduce's thresholds, eps / 4 per level), made on the device."""
+        h = ctypes.c_void_p()
+        rc = _native.lib().dplr_gpu_plan_reduce_svd(self._h, float(eps), int(workers), _stream_ptr(stream),
+                                                     ctypes.byref(h))
+        if not h.value:
+            _native.check(rc, "dplr_gpu_plan_reduce_svd")
+        return GpuPlan(None, _handle=h)
+
     def to_dense(self, stream=None) -> torch.Tensor:
         """The dense m x m matrix on the device (dplrgep2d), as a (m, m)
         tensor whose row j is column j of the matrix."""

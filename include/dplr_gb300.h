@@ -92,6 +92,22 @@ DPLR_API int dplr_gpu_adpy(dplr_gpu_plan plan, double alpha, const double *D, vo
 DPLR_API int dplr_gpu_plan_copy(dplr_gpu_plan plan, void *stream, dplr_gpu_plan *out);
 DPLR_API int dplr_gpu_axpy(double alpha, dplr_gpu_plan A, dplr_gpu_plan B, void *stream, dplr_gpu_plan *out);
 DPLR_API int dplr_gpu_gep2d(dplr_gpu_plan plan, double *D, long long ldd, void *stream);
+/* SVD recompression of a device plan (dplr_gpu_reduce_svd without host
+ * trees): *out is a new plan in which every low-rank block is its truncated
+ * SVD with the singular values >= eps / 4^(depth+1) (dplrreduce's split,
+ * src/dplrreduce.c:46); leaves are copied.  Ranks only shrink.  workers as
+ * for dplr_gpu_reduce_svd.  DPLR_GPU_ENOTCONV (with *out valid) if an SVD
+ * did not converge; that block is kept. */
+DPLR_API int dplr_gpu_plan_reduce_svd(dplr_gpu_plan plan, double eps, int workers, void *stream,
+                                      dplr_gpu_plan *out);
+
+/* Recompression after the operations that grow ranks, off by default (DPLR
+ * never recompresses, quirk Q2).  With eps >= 0, dplraxpy, dplrgeprk,
+ * dplrgeinv, dplrgeppmm / dplr_gpu_geppmm run dplr_gpu_reduce_svd(m, out,
+ * eps) on their output tree, and dplr_gpu_axpy returns its plan
+ * recompressed by dplr_gpu_plan_reduce_svd with eps.  eps < 0 turns it off.
+ * Process-wide. */
+DPLR_API void dplr_gpu_set_recompress(double eps);
 
 /* Woodbury factorisation of the planned matrix (replaces forming inv(A)
  * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):

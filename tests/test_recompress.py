@@ -135,3 +135,93 @@ def test_gpu_rejects_invalid_arguments():
         assert lib.dplr_gpu_reduce_svd(32, c, 1e-8, 0) == -1
     finally:
         tree.free_c(c)
+
+
+# ----------------------------------------------------- device plans -------
+
+def _plan_tree(plan, like):
+    """Blocks of a plan read back from its pool, shaped like `like`."""
+    pool = plan.read_pool().cpu().numpy()
+    blocks = plan.pool_blocks()
+    lr = iter([b for b in blocks if b["kind"] == "lowrank"])
+    lf = iter([b for b in blocks if b["kind"] == "leaf"])
+
+    def walk(node):
+        if isinstance(node, tree.Dense):
+            b = next(lf)
+            n = b["b"]
+            return tree.Dense(pool[b["d"]:b["d"] + n * n].reshape(n, n, order="F"))
+        out = []
+        for blk in (next(lr), next(lr)):
+            n, r = blk["n"], blk["rank"]
+            out.append(tree.LowRank(pool[blk["u"]:blk["u"] + n * r].reshape(n, r, order="F"),
+                                    pool[blk["sig"]:blk["sig"] + r].copy(),
+                                    pool[blk["v"]:blk["v"] + n * r].reshape(n, r, order="F")))
+        return tree.HNode(walk(node.nw), out[0], walk(node.se), out[1])
+
+    return walk(like)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eps", [1e-9, 1e-4])
+def test_plan_recompression_matches_the_host_tree_one(eps):
+    """dplr_gpu_plan_reduce_svd on a device plan gives the blocks
+    dplr_gpu_reduce_svd gives on the host tree (same ranks, same truncated
+    products), with no host round trip."""
+    from dplr_gb300.plan import GpuPlan
+    t = _doubled(gen.random_tree(1024, 64, [9, 7, 5, 3], seed=5, diag_shift=2.0, decay=0.3))
+    p = GpuPlan(t)
+    r = p.reduce_svd(eps)
+    got = _plan_tree(r, t)
+    want = _gpu(t, eps)
+    for (g, _), (w, _) in zip(_blocks(got, eps=1.0), _blocks(want, eps=1.0)):
+        assert g.rank == w.rank
+        if w.rank:
+            scale = max(1.0, float(w.sig[0]))
+            np.testing.assert_allclose(g.sig, w.sig, rtol=0, atol=1e-12 * scale)
+            np.testing.assert_allclose((g.u * g.sig) @ g.v.T, (w.u * w.sig) @ w.v.T, rtol=0, atol=1e-12 * scale)
+    x = np.random.default_rng(0).standard_normal((3, t.size))
+    import torch
+    y = r.apply(torch.tensor(x, device="cuda")).cpu().numpy()
+    yw = (tree.to_dense(want) @ x.T).T
+    assert np.linalg.norm(y - yw) <= 1e-12 * np.linalg.norm(yw)
+    p.close()
+    r.close()
+
+
+@pytest.mark.gpu
+def test_recompression_after_rank_growing_operations():
+    """Off by default (DPLR never recompresses): dplraxpy of A into a copy of
+    A doubles every rank.  With dplr_gpu_set_recompress(eps) the host drop-in
+    and the device dplr_gpu_axpy both return the recompressed sum 2 A, at A's
+    ranks."""
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+    lib, api = _native.lib(), _native.api()
+    a = gen.random_tree(512, 32, [6, 4, 3], seed=9, diag_shift=2.0, decay=0.3)
+    ranks_a = tree.ranks_by_level(a)
+
+    def host_axpy():
+        ca, cb = tree.to_c(a), tree.to_c(a)
+        api.axpy(a.size, 1.0, ca, cb)
+        out = tree.from_c(cb)
+        tree.free_c(ca)
+        tree.free_c(cb)
+        return out
+
+    try:
+        grown = host_axpy()
+        assert tree.ranks_by_level(grown) == [2 * r for r in ranks_a]
+        lib.dplr_gpu_set_recompress(1e-9)
+        reduced = host_axpy()
+        assert tree.ranks_by_level(reduced) == ranks_a
+        np.testing.assert_allclose(tree.to_dense(reduced), 2.0 * tree.to_dense(a), atol=1e-11)
+        pa = GpuPlan(a)
+        pc = pa.axpy(1.0, pa)
+        got = _plan_tree(pc, a)
+        assert tree.ranks_by_level(got) == ranks_a
+        np.testing.assert_allclose(tree.to_dense(got), 2.0 * tree.to_dense(a), atol=1e-11)
+        pa.close()
+        pc.close()
+    finally:
+        lib.dplr_gpu_set_recompress(-1.0)
