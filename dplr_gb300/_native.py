@@ -100,6 +100,7 @@ _OPTIONAL: list = [
     ("dplr_gpu_gep2d", c_int, [c_void_p, c_void_p, c_longlong, c_void_p]),
     ("dplr_gpu_plan_reduce_svd", c_int, [c_void_p, c_double, c_int, c_void_p, POINTER(c_void_p)]),
     ("dplr_gpu_set_recompress", None, [c_double]),
+    ("dplr_gpu_apply_form", c_int, [c_void_p]),
 ]
 
 

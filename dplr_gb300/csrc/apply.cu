@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
             }
             __syncthreads();
 #pragma unroll 4
-            for (int r = g; r < S; r += G) {
+            for (int r = g; r < ns; r += G) {             // live rows only: short chunks stay cheap
                 double f = Fs[r * (RT + 1) + kk];
 #pragma unroll
                 for (int j = 0; j < NB; ++j) acc[j] = fma(f, Xs[r * NB + j], acc[j]);
@@ -639,8 +639,11 @@ int apply_device(Plan *p, int trans, int nrhs, double alpha, const double *X, in
     if (pairs_usable(p, trans, nrhs)) return pairs_apply(p, alpha, X, beta, Y, st);
     // one persistent launch unless DPLR_GB300_APPLY=launches asks for the
     // three-launch form (panel, reduce, expand)
+    // three launches when the autotuner found them faster for this plan
+    // (many tiny blocks), or when DPLR_GB300_APPLY=launches asks for them
     const char *mode = getenv("DPLR_GB300_APPLY");
-    if (!(mode && !strcmp(mode, "launches")) && persist_usable(p, trans, nrhs))
+    const bool launches = mode ? !strcmp(mode, "launches") : p->apply_launches != 0;
+    if (!launches && persist_usable(p, trans, nrhs))
         return persist_apply(p, trans, nrhs, alpha, X, ldx, beta, Y, ldy, st);
     const Schedule &S = p->sched[trans ? 1 : 0];
     size_t need = (size_t)(S.t_per_rhs + S.partial_per_rhs) * nrhs;

@@ -135,6 +135,12 @@ int dplr_gpu_graph_launch(dplr_gpu_graph graph, void *stream)
     return 0;
 }
 
+int dplr_gpu_apply_form(dplr_gpu_plan plan)
+{
+    const Plan *p = (const Plan *)plan;
+    return p ? p->apply_launches : fail(DPLR_GPU_EINVAL, "dplr_gpu_apply_form: null plan");
+}
+
 long long dplr_gpu_graph_kernels(dplr_gpu_graph graph)
 {
     return graph ? ((GraphH *)graph)->kernels : 0;
@@ -168,7 +174,7 @@ int dplr_gpu_autotune(dplr_gpu_plan plan, int n, void *stream, int *chunk_rows, 
     cudaEventCreate(&e1);
     const int chunks[] = {256, 512, 1024, 2048};
     const int caps[] = {1, 2, 4, 8, 16};
-    int best_c = p->chunk_rows, best_nb = p->nb_cap;
+    int best_c = p->chunk_rows, best_nb = p->nb_cap, best_form = p->apply_launches;
     float best = 1e30f;
     for (int c : chunks) {
         if (rc) break;
@@ -177,29 +183,37 @@ int dplr_gpu_autotune(dplr_gpu_plan plan, int n, void *stream, int *chunk_rows, 
         for (int nb : caps) {
             if (nb > 1 && nb > n) break;
             set_nb_cap(p, nb);
-            if ((rc = apply_device(p, 0, n, 1.0, X, p->m, 0.0, Y, p->m, st, false))) break;
-            cudaEventRecord(e0, st);
-            for (int r = 0; r < 3 && !rc; ++r) rc = apply_device(p, 0, n, 1.0, X, p->m, 0.0, Y, p->m, st, false);
-            cudaEventRecord(e1, st);
+            // both forms of the apply: one persistent launch, three launches
+            for (int form = 0; form < 2 && !rc; ++form) {
+                p->apply_launches = form;
+                if ((rc = apply_device(p, 0, n, 1.0, X, p->m, 0.0, Y, p->m, st, false))) break;
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < 3 && !rc; ++r)
+                    rc = apply_device(p, 0, n, 1.0, X, p->m, 0.0, Y, p->m, st, false);
+                cudaEventRecord(e1, st);
+                if (rc) break;
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    rc = fail(DPLR_GPU_ECUDA, "dplr_gpu_autotune: timing failed");
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= 3.f;
+                if (ms < best) {
+                    best = ms;
+                    best_c = c;
+                    best_nb = nb;
+                    best_form = form;
+                }
+            }
             if (rc) break;
-            if (cudaEventSynchronize(e1) != cudaSuccess) {
-                rc = fail(DPLR_GPU_ECUDA, "dplr_gpu_autotune: timing failed");
-                break;
-            }
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= 3.f;
-            if (ms < best) {
-                best = ms;
-                best_c = c;
-                best_nb = nb;
-            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(buf);
     p->chunk_rows = best_c;
+    p->apply_launches = best_form;
     int rc2 = plan_reschedule(p);
     set_nb_cap(p, best_nb);
     if (rc) return rc;

@@ -179,6 +179,7 @@ struct Plan {
     double *xbuf = nullptr, *ybuf = nullptr;   // host<->device staging for drop-in
     size_t xbuf_doubles = 0, ybuf_doubles = 0;
     int chunk_rows = 512;
+    int apply_launches = 0;           // 1: the autotuner chose the three-launch apply over the persistent one
     long long device_bytes = 0;
     // Woodbury factorisation (filled by factor.cu)
     void *fact = nullptr;
@@ -190,11 +191,6 @@ struct Plan {
     int *tc_err_h = nullptr, *tc_err_d = nullptr;
     // float-pair copy of the factors for the 1-RHS apply (pairs.cu)
     void *pairs = nullptr;
-    // host <-> device copies of the refined host solve split over streams
-    // (one copy engine each), created on first use (solve.cu)
-    static constexpr int kCopyStreams = 4;
-    cudaStream_t copy_st[kCopyStreams] = {};
-    cudaEvent_t copy_ev[kCopyStreams + 1] = {};
     // factor gradients (grad.cu): work lists and scratch
     void *grad = nullptr;
     double *gbuf = nullptr;

@@ -103,7 +103,7 @@ __device__ void panel_unit(const Args &a, const PanelItem &it, int jt, double *s
             }
             __syncthreads();
 #pragma unroll 4
-            for (int r = g; r < S; r += G) {
+            for (int r = g; r < ns; r += G) {             // live rows only: short chunks stay cheap
                 const double f = Fs[r * (RT + 1) + kk];
 #pragma unroll
                 for (int j = 0; j < NB; ++j) acc[j] = fma(f, Xs[r * NB + j], acc[j]);

@@ -448,10 +448,6 @@ void plan_free(Plan *p)
     cudaFree(p->xbuf);
     cudaFree(p->ybuf);
     if (p->tc_err_h) cudaFreeHost(p->tc_err_h);
-    for (cudaStream_t s : p->copy_st)
-        if (s) cudaStreamDestroy(s);
-    for (cudaEvent_t e : p->copy_ev)
-        if (e) cudaEventDestroy(e);
     grad_free(p);
     cudaFree(p->gbuf);
     delete p;

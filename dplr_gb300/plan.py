@@ -95,7 +95,9 @@ class GpuPlan:
         c, nb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         _native.check(_native.lib().dplr_gpu_autotune(self._h, int(n), _stream_ptr(stream), ctypes.byref(c),
                                                       ctypes.byref(nb), ctypes.byref(ms)), "dplr_gpu_autotune")
-        return {"chunk_rows": c.value, "nb_cap": nb.value, "apply_ms": ms.value}
+        form = _native.lib().dplr_gpu_apply_form(self._h)
+        return {"chunk_rows": c.value, "nb_cap": nb.value, "apply_ms": ms.value,
+                "apply_form": "three launches" if form == 1 else "persistent"}
 
     def prepare_mixed(self, slices: int = 7, fp64_capacitance: bool = False, stream=None) -> None:
         """Sliced factor copies (3 to 7 bf16 slices) for the low-precision inner

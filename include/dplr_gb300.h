@@ -250,12 +250,14 @@ DPLR_API long long dplr_gpu_graph_kernels(dplr_gpu_graph graph);
 DPLR_API void dplr_gpu_graph_destroy(dplr_gpu_graph graph);
 
 /* Launch-shape autotuner of the FP64 kernels: times the apply with n
- * right-hand sides for every panel chunk length (256 to 2048 rows) and
- * right-hand-side tile (1 to 16 columns) and keeps the fastest in the plan.
- * Call it before dplr_gpu_factor for the solve sweeps to use the tuned
- * chunk length. */
+ * right-hand sides for every panel chunk length (256 to 2048 rows),
+ * right-hand-side tile (1 to 16 columns) and form (one persistent launch or
+ * three launches) and keeps the fastest in the plan.  Call it before
+ * dplr_gpu_factor for the solve sweeps to use the tuned chunk length.
+ * dplr_gpu_apply_form reports the form kept: 0 persistent, 1 three launches. */
 DPLR_API int dplr_gpu_autotune(dplr_gpu_plan plan, int n, void *stream, int *chunk_rows, int *nb_cap,
                                double *best_ms);
+DPLR_API int dplr_gpu_apply_form(dplr_gpu_plan plan);
 
 /* Instrumentation.  dplr_gpu_launch_count: kernels launched by this
  * library since load.  Between dplr_gpu_profile_start() and
