@@ -71,3 +71,35 @@ def test_noalloc_apply_rejects_oversized_request():
     assert rc == -1
     assert "static scratch" in _native.last_error()
     p.close()
+
+
+def test_noalloc_apply_allocates_nothing():
+    """The property callers rely on: with every device allocation the library
+    might make set up to fail (the fault-injection hook), the call on a
+    fresh plan, which has no apply scratch of its own yet, still succeeds,
+    gives the same result, and leaves the plan's device memory unchanged."""
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+    f = _noalloc_fn()
+    lib = _native.lib()
+    t = gen.random_tree(1024, 64, [20, 12, 6, 3], seed=33)
+    m = t.size
+    stream = torch.cuda.current_stream().cuda_stream
+    x = torch.randn(3, m, dtype=torch.float64, device="cuda")
+    ref = GpuPlan(t)
+    want = ref.apply(x)
+    fresh = GpuPlan(t)
+    before = lib.dplr_gpu_plan_device_bytes(fresh.handle)
+    got = torch.zeros_like(x)
+    torch.cuda.synchronize()
+    try:
+        lib.dplr_gpu_debug_fail_alloc(0)          # the next library allocation would fail
+        rc = f(fresh.handle, b"N", 3, 1.0, x.data_ptr(), m, 0.0, got.data_ptr(), m, stream)
+        torch.cuda.synchronize()
+    finally:
+        lib.dplr_gpu_debug_fail_alloc(-1)
+    assert rc == 0, _native.last_error()
+    assert rel(got, want) <= TOL
+    assert lib.dplr_gpu_plan_device_bytes(fresh.handle) == before
+    fresh.close()
+    ref.close()
