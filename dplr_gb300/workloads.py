@@ -192,103 +192,142 @@ def batched_trees(count: int = 512, seed: int = 0):
     return trees, nrhs
 
 
+RHS_BUCKETS = (2, 4, 8, 16)
+
+
 def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
+    """The 512 matrices grouped by their right-hand-side count into batch
+    plans of at most 2, 4, 8 and 16 stacked columns (so a matrix with one
+    right-hand side does not pay for 16); each plan is autotuned and
+    factored, and one step replays every plan's apply graph and
+    refined-solve graph."""
     t0 = time.time()
     trees, nrhs = batched_trees(count)
     t_gen = time.time() - t0
-    t0 = time.time()
-    plan = GpuPlan.batch(trees)
-    t_up = time.time() - t0
-    n = max(nrhs)
-    tune = plan.autotune(n)
-    torch.cuda.synchronize()
-    t0 = time.time()
-    plan.factor()
-    torch.cuda.synchronize()
-    t_fac = time.time() - t0
-    offs = plan.offsets()
-    X = torch.zeros(n, plan.m, dtype=torch.float64, device="cuda")
+    groups = []
+    lo = 0
+    for hi in RHS_BUCKETS:
+        idx = [i for i, k in enumerate(nrhs) if lo < k <= hi]
+        lo = hi
+        if idx:
+            groups.append({"idx": idx, "n": max(nrhs[i] for i in idx)})
+    t_up = t_fac = 0.0
     g = torch.Generator(device="cuda").manual_seed(5)
-    for o, t, k in zip(offs, trees, nrhs):     # matrix i uses its first nrhs_i columns
-        X[:k, o:o + t.size] = torch.randn(k, t.size, generator=g, dtype=torch.float64, device="cuda")
-    Y = torch.empty_like(X)
-    Z = torch.empty_like(X)
-    ga = GpuGraph(plan, "A", X, Y)
-    gs = GpuGraph(plan, "R", X, Z)                # solve + two FP64-residual corrections, one replay
+    for grp in groups:
+        gt = [trees[i] for i in grp["idx"]]
+        t0 = time.time()
+        plan = GpuPlan.batch(gt)
+        t_up += time.time() - t0
+        grp["tune"] = plan.autotune(grp["n"])
+        torch.cuda.synchronize()
+        t0 = time.time()
+        plan.factor()
+        torch.cuda.synchronize()
+        t_fac += time.time() - t0
+        X = torch.zeros(grp["n"], plan.m, dtype=torch.float64, device="cuda")
+        for o, i in zip(plan.offsets(), grp["idx"]):       # matrix i uses its first nrhs_i columns
+            X[:nrhs[i], o:o + trees[i].size] = torch.randn(nrhs[i], trees[i].size, generator=g,
+                                                           dtype=torch.float64, device="cuda")
+        grp.update(plan=plan, X=X, Y=torch.empty_like(X), Z=torch.empty_like(X))
+        grp["ga"] = GpuGraph(plan, "A", X, grp["Y"])
+        grp["gs"] = GpuGraph(plan, "R", X, grp["Z"])       # solve + two FP64-residual corrections
+
+    def step():
+        for grp in groups:
+            grp["ga"].launch()
+            grp["gs"].launch()
+
     stream = torch.cuda.current_stream()
     for _ in range(max(3, warmup)):
-        ga.launch()
-        gs.launch()
+        step()
     torch.cuda.synchronize()
     l0 = _native.launch_count()
     e0, e1 = _events()
     e0.record(stream)
     for _ in range(steps):
-        ga.launch()
-        gs.launch()
+        step()
     e1.record(stream)
     torch.cuda.synchronize()
     launches = _native.launch_count() - l0
     ms = e0.elapsed_time(e1) / steps
-    # the same step once more, launch by launch, for its algorithmic FP64
-    # flops and per-kernel times (graph replays carry no events)
-    _native.profile_start()
-    plan.apply(X, out=Y)
-    prof = _native.profile_stop()
-    _native.profile_start()
-    _refined_once(plan, X, Z)
-    prof_s = _native.profile_stop()
-    flops = sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_s.values())
+    # algorithmic FP64 flops of one step, launch by launch (graph replays
+    # carry no events), counted on the right-hand sides the matrices have:
+    # each group's stacked count scaled by its real columns
+    flops, kern = 0.0, {}
+    for grp in groups:
+        plan = grp["plan"]
+        _native.profile_start()
+        plan.apply(grp["X"], out=grp["Y"])
+        _refined_once(plan, grp["X"], grp["Z"])
+        prof = _native.profile_stop()
+        real = sum(nrhs[i] for i in grp["idx"]) / (grp["n"] * len(grp["idx"]))
+        flops += real * sum(v[1] for v in prof.values())
+        for k, v in prof.items():
+            kern[k] = kern.get(k, 0.0) + v[0]
     fp64 = fp64_gemm_peak()
     tflops = flops / (ms / 1e3) / 1e12
     # accuracy of every matrix's own right-hand sides, from the exact-slice
     # residual of the replayed refined solve (FP64 residuals cannot resolve
-    # below ~1e-12 on the longer length scales)
-    plan.prepare_sliced()
+    # below ~1e-12 on the longer length scales); and the same graph with
+    # exact-slice residuals in its corrections
+    worst, exact_worst, exact_ms, exact_kernels = 0.0, 0.0, 0.0, 0
+    for grp in groups:
+        plan = grp["plan"]
+        plan.prepare_sliced()
 
-    def worst_resid(Zs):
-        R = plan.residual(Zs, X, precise=True)
-        w = 0.0
-        for o, t, k in zip(offs, trees, nrhs):
-            rn = R[:k, o:o + t.size].norm(dim=1)
-            bn = X[:k, o:o + t.size].norm(dim=1)
-            w = max(w, float((rn / bn).max()))
-        return w
+        def worst_resid(Zs):
+            R = plan.residual(Zs, grp["X"], precise=True)
+            w = 0.0
+            for o, i in zip(plan.offsets(), grp["idx"]):
+                k, n_i = nrhs[i], trees[i].size
+                w = max(w, float((R[:k, o:o + n_i].norm(dim=1) / grp["X"][:k, o:o + n_i].norm(dim=1)).max()))
+            return w
 
-    worst = worst_resid(Z)
-    # the same graph with exact-slice residuals in its two corrections
-    Z2 = torch.empty_like(X)
-    gx = GpuGraph(plan, "R", X, Z2)
-    gx.launch()
-    torch.cuda.synchronize()
-    e0, e1 = _events()
-    e0.record(stream)
-    gx.launch()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    exact = {"ms": e0.elapsed_time(e1), "max_rel_resid": worst_resid(Z2), "kernels": gx.kernels,
-             "note": "refined-solve graph whose corrections use exact-slice residuals (mma.sync kernels "
-                     "for these leaf-64 matrices)"}
-    gx.close()
+        worst = max(worst, worst_resid(grp["Z"]))
+        Z2 = torch.empty_like(grp["X"])
+        gx = GpuGraph(plan, "R", grp["X"], Z2)
+        gx.launch()
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record(stream)
+        gx.launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        exact_ms += e0.elapsed_time(e1)
+        exact_kernels += gx.kernels
+        exact_worst = max(exact_worst, worst_resid(Z2))
+        gx.close()
     total_rhs = sum(nrhs)
-    return {
+    out = {
         "metric": "batched PLR apply+refined solve RHS/s (512 matrices, uneven N/rank/RHS, graph replay)",
         "value": 2.0 * total_rhs / (ms / 1e3), "unit": "RHS/s", "ms_per_step": ms,
         "higher_is_better": True, "dtype": "f64", "gpu_launches": launches,
-        "roofline": {"kernel": "whole step (apply graph + refined-solve graph)", "bound": "fp64",
+        "roofline": {"kernel": "whole step (apply graphs + refined-solve graphs)", "bound": "fp64",
                      "achieved": tflops, "peak": fp64["tflops"], "unit": "TFLOP/s",
                      "frac": tflops / fp64["tflops"], "traffic": None, "peak_source": "of " + fp64["source"],
-                     "algorithmic": f"{flops:.4g} flop per step (sum of the launches' algorithmic counts, "
-                                    f"stacked right-hand sides)"},
+                     "algorithmic": f"{flops:.4g} flop per step (the launches' algorithmic counts, scaled to "
+                                    f"the right-hand sides each matrix has)"},
         "config": {"workload": "512 1D exponential-kernel PLR matrices, N in [1024, 16384], leaf 64, "
-                               "ranks 1-4, 1-16 RHS each; one apply graph + one refined-solve graph (two corrections) per step",
-                   "matrices": count, "rows_total": plan.m, "rhs_total": total_rhs, "rhs_stacked": n,
-                   "graph_kernels": {"apply": ga.kernels, "refined_solve": gs.kernels},
-                   "autotune": tune, "refined_solve_max_rel_resid": worst,
-                   "refined_solve_exact_residual": exact,
-                   "kernels_ms": {k: v[0] for k, v in {**prof_s}.items()},
+                               "ranks 1-4, 1-16 RHS each, grouped by RHS count into batch plans of <= 2, 4, 8, "
+                               "16 columns; per step every plan's apply graph and refined-solve graph "
+                               "(two corrections)",
+                   "matrices": count, "rows_total": sum(t.size for t in trees), "rhs_total": total_rhs,
+                   "groups": [{"matrices": len(grp["idx"]), "rhs_stacked": grp["n"],
+                               "graph_kernels": {"apply": grp["ga"].kernels, "refined_solve": grp["gs"].kernels},
+                               "autotune": grp["tune"]} for grp in groups],
+                   "refined_solve_max_rel_resid": worst,
+                   "refined_solve_exact_residual": {
+                       "ms": exact_ms, "max_rel_resid": exact_worst, "kernels": exact_kernels,
+                       "note": "the same refined-solve graphs with exact-slice residuals in the corrections "
+                               "(mma.sync kernels for these leaf-64 matrices)"},
+                   "kernels_ms": kern,
                    "setup_s": {"generate": t_gen, "upload": t_up, "factor": t_fac}},
     }
+    for grp in groups:
+        grp["ga"].close()
+        grp["gs"].close()
+        grp["plan"].close()
+    return out
 
 
 def _refined_once(plan, b, x):
