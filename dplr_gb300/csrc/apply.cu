@@ -15,7 +15,6 @@
 // more than a few right-hand sides the kernels are FP64-issue bound; the
 // smem staging only has to keep HBM traffic low, not feed tensor cores.
 #include "internal.cuh"
-#include "panel_small.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -48,11 +47,6 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
     const double *F = fbase + it.f;
     const int j0 = blockIdx.y * NB;
     const int nj = min(NB, nrhs - j0);
-    if (it.rank <= kSmallRank) {              // rows per thread, all ranks in registers
-        panel_small_rank<NB>(F, it.n, it.r0, it.len, it.rank, X, ldx, it.in0, j0, nj,
-                             partials + it.p * nrhs + (long long)it.chunk * it.rank * nrhs, sm);
-        return;
-    }
     int RT = 8;
     while (RT < it.rank && RT < kRankTile) RT <<= 1;
     const int G = kThreads / RT, S = 4 * G;
@@ -121,11 +115,6 @@ __global__ void __launch_bounds__(kThreads) panel1_kernel(const PanelItem *__res
 {
     __shared__ __align__(16) double xs[kPanel1MaxLen];
     const PanelItem it = items[blockIdx.x];
-    if (it.rank <= kSmallRank) {              // rows per thread, all ranks in registers
-        panel_small_rank<1>(fbase + it.f, it.n, it.r0, it.len, it.rank, X, 0, it.in0, 0, 1,
-                            partials + it.p + (long long)it.chunk * it.rank, xs);
-        return;
-    }
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     for (int r = t; r < it.len; r += kThreads) xs[r] = X[it.in0 + it.r0 + r];
     __syncthreads();

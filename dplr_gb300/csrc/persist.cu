@@ -24,7 +24,6 @@
 // right-hand side uses warp-per-column panels with 16-byte loads and
 // shuffle reductions; more use shared-memory staged tiles of NB columns.
 #include "internal.cuh"
-#include "panel_small.cuh"
 
 #include <algorithm>
 
@@ -75,11 +74,6 @@ template <int NB>
 __device__ void panel_unit(const Args &a, const PanelItem &it, int jt, double *sm)
 {
     const int j0 = jt * NB, nj = min(NB, a.nrhs - j0);
-    if (it.rank <= kSmallRank) {              // rows per thread, all ranks in registers
-        panel_small_rank<NB>(a.pool + it.f, it.n, it.r0, it.len, it.rank, a.X, a.ldx, it.in0, j0, nj,
-                             a.partials + it.p * a.nrhs + (long long)it.chunk * it.rank * a.nrhs, sm);
-        return;
-    }
     int RT = 8;
     while (RT < it.rank && RT < 64) RT <<= 1;
     const int G = kPT / RT, S = 8 * G;
@@ -136,11 +130,6 @@ __device__ void panel_unit(const Args &a, const PanelItem &it, int jt, double *s
 // reduction of the four column sums.
 __device__ void panel_unit1(const Args &a, const PanelItem &it, double *sm)
 {
-    if (it.rank <= kSmallRank) {              // rows per thread, all ranks in registers
-        panel_small_rank<1>(a.pool + it.f, it.n, it.r0, it.len, it.rank, a.X, 0, it.in0, 0, 1,
-                            a.partials + it.p + (long long)it.chunk * it.rank, sm);
-        return;
-    }
     double *xs = sm;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     for (int r = t; r < it.len; r += kPT) xs[r] = __ldg(a.X + it.in0 + it.r0 + r);
