@@ -15,6 +15,7 @@
 // more than a few right-hand sides the kernels are FP64-issue bound; the
 // smem staging only has to keep HBM traffic low, not feed tensor cores.
 #include "internal.cuh"
+#include "panel_rank4.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -42,11 +43,17 @@ __global__ void __launch_bounds__(kThreads) panel_kernel(
     constexpr int kStage = 1152 + 128 * NB;
     constexpr int kRed = kThreads * NB;
     __shared__ double sm[kStage > kRed ? kStage : kRed];
+    static_assert(rank4_smem<NB>(kThreads) <= (kStage > kRed ? kStage : kRed), "rank <= 4 panel scratch");
 
     const PanelItem it = items[blockIdx.x];
     const double *F = fbase + it.f;
     const int j0 = blockIdx.y * NB;
     const int nj = min(NB, nrhs - j0);
+    if (it.rank <= kRank4) {                  // every FMA live: threads own right-hand sides
+        panel_rank4<NB>(F, it.n, it.r0, it.len, it.rank, X, ldx, it.in0, j0, nj,
+                        partials + it.p * nrhs + (long long)it.chunk * it.rank * nrhs, sm);
+        return;
+    }
     int RT = 8;
     while (RT < it.rank && RT < kRankTile) RT <<= 1;
     const int G = kThreads / RT, S = 4 * G;

@@ -163,6 +163,7 @@ struct Plan {
     int m = 0, levels = 0, max_rank = 0, total_rank = 0;
     int ntrees = 1;                   // > 1: a batch of independent trees (block diagonal)
     std::vector<int> tree_row0;       // first row of every tree
+    int *d_tree_row0 = nullptr;       // device copy + m (batch plans, built on first refined solve)
     int nb_cap = 16;                  // largest right-hand-side tile of the FP64 kernels (autotuned)
     long long nnz = 0;
     std::vector<LRDesc> lr;

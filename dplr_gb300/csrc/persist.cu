@@ -24,6 +24,7 @@
 // right-hand side uses warp-per-column panels with 16-byte loads and
 // shuffle reductions; more use shared-memory staged tiles of NB columns.
 #include "internal.cuh"
+#include "panel_rank4.cuh"
 
 #include <algorithm>
 
@@ -74,6 +75,11 @@ template <int NB>
 __device__ void panel_unit(const Args &a, const PanelItem &it, int jt, double *sm)
 {
     const int j0 = jt * NB, nj = min(NB, a.nrhs - j0);
+    if (it.rank <= kRank4) {                  // every FMA live: threads own right-hand sides
+        panel_rank4<NB>(a.pool + it.f, it.n, it.r0, it.len, it.rank, a.X, a.ldx, it.in0, j0, nj,
+                        a.partials + it.p * a.nrhs + (long long)it.chunk * it.rank * a.nrhs, sm);
+        return;
+    }
     int RT = 8;
     while (RT < it.rank && RT < 64) RT <<= 1;
     const int G = kPT / RT, S = 8 * G;
@@ -394,6 +400,7 @@ constexpr size_t smem_bytes()
     // reductions: 256 x NB (panel, expand) and 8 x 33 (reduce)
     constexpr size_t p = 256 * 9 + 256 * NB, e = 64 * (kExpSlab + 1) + kExpSlab * NB, r = kPT * NB;
     constexpr size_t m1 = p > e ? p : e, m2 = m1 > r ? m1 : r;
+    static_assert((size_t)rank4_smem<NB>(kPT) <= m2, "rank <= 4 panel scratch");
     return (NB == 1 ? (size_t)kX1Max > m2 ? (size_t)kX1Max : m2 : m2) * sizeof(double);
 }
 

@@ -442,6 +442,7 @@ void plan_free(Plan *p)
     cudaFree(p->pool);
     cudaFree(p->d_lr);
     cudaFree(p->d_leaves);
+    cudaFree(p->d_tree_row0);
     free_schedule(p->sched[0]);
     free_schedule(p->sched[1]);
     cudaFree(p->work);

@@ -37,6 +37,28 @@ __global__ void colnorm_kernel(const double *A, int m, int lda, double *out)
     if (threadIdx.x == 0) out[blockIdx.x] = sqrt(red[0]);
 }
 
+// Column 2-norms per tree of a batch: out[j * nseg + t] over the rows
+// [row0[t], row0[t + 1]) of column j; one CTA per (tree, column).
+__global__ void segnorm_kernel(const double *A, int lda, int n, const int *row0, int nseg, double *out)
+{
+    __shared__ double red[256];
+    const int t = blockIdx.x;
+    const int r0 = row0[t], r1 = row0[t + 1];
+    for (int j = blockIdx.y; j < n; j += gridDim.y) {
+        const double *a = A + (long long)j * lda;
+        double s = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) s = fma(a[i], a[i], s);
+        __syncthreads();                 // red is reused across columns
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+            if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[(long long)j * nseg + t] = sqrt(red[0]);
+    }
+}
+
 // Y (m x n) := X + alpha*Y  or plain copies, column-major with leading dims.
 __global__ void axpby_kernel(int m, int n, double a, const double *X, int ldx, double b, double *Y,
                              int ldy)
@@ -93,6 +115,25 @@ int colnorms_device(const double *A, int m, int n, int lda, double *out, cudaStr
 {
     if (n <= 0) return 0;
     colnorm_kernel<<<n, 256, 0, st>>>(A, m, lda, out);
+    note_launch();
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Norms of every column of every tree: nseg = 1 for one tree (plain column
+// norms), else per tree of the batch, out[j * nseg + t].
+static int segnorms_device(Plan *p, const double *A, int n, int lda, double *out, cudaStream_t st)
+{
+    if (p->ntrees <= 1) return colnorms_device(A, p->m, n, lda, out, st);
+    if (n <= 0) return 0;
+    if (!p->d_tree_row0) {
+        std::vector<int> rows(p->tree_row0);
+        rows.push_back(p->m);
+        DG_ALLOC(&p->d_tree_row0, rows.size() * sizeof(int));
+        DG_CUDA(cudaMemcpy(p->d_tree_row0, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    segnorm_kernel<<<dim3((unsigned)p->ntrees, (unsigned)std::min(n, 65535)), 256, 0, st>>>(
+        A, lda, n, p->d_tree_row0, p->ntrees, out);
     note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;
@@ -181,13 +222,16 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
     }
     cudaStream_t st = (cudaStream_t)stream;
     const int m = p->m;
-    // Scratch: residual R, correction D (m x n each), 2n norms.
-    size_t need = (size_t)2 * m * n + 2 * (size_t)n;
+    // Scratch: residual R, correction D (m x n each), the norms of B and R
+    // per column and tree: a batch converges when every tree's every column
+    // does, not on the norms of the stacked columns.
+    const size_t nn = (size_t)n * std::max(p->ntrees, 1);
+    size_t need = (size_t)2 * m * n + 2 * nn;
     int rc = ensure_buffer(&p->ybuf, &p->ybuf_doubles, need);
     if (rc) return rc;
     double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
-    double *bn = D + (size_t)m * n, *rn = bn + n;
-    std::vector<double> hb(n), hr(n);
+    double *bn = D + (size_t)m * n, *rn = bn + nn;
+    std::vector<double> hb(nn), hr(nn);
     const bool mixed = (flags & DPLR_GPU_SOLVE_MIXED) != 0;
     if (mixed && !p->mixed) return fail(DPLR_GPU_ESTATE, "solve: mixed solve not prepared");
     if ((flags & DPLR_GPU_RESIDUAL_SLICED) && !p->sliced)
@@ -195,8 +239,8 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
     auto inner = [&](const double *rhs, int ld, double *out, int ldo) -> int {
         return mixed ? mixed_solve(p, n, rhs, ld, out, ldo, st) : factor_solve(p, 0, n, rhs, ld, out, ldo, st);
     };
-    if ((rc = colnorms_device(B, m, n, ldb, bn, st))) return rc;
-    DG_CUDA(cudaMemcpyAsync(hb.data(), bn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if ((rc = segnorms_device(p, B, n, ldb, bn, st))) return rc;
+    DG_CUDA(cudaMemcpyAsync(hb.data(), bn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
     if ((rc = inner(B, ldb, X, ldx))) return rc;
     double worst = INFINITY;
     int it = 0;
@@ -210,13 +254,13 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
         }
         {
             ProfScope ps("refine_norms", st, 0.0, 8.0 * m * n);
-            if ((rc = colnorms_device(R, m, n, m, rn, st))) return rc;
+            if ((rc = segnorms_device(p, R, n, m, rn, st))) return rc;
         }
-        DG_CUDA(cudaMemcpyAsync(hr.data(), rn, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(hr.data(), rn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
         DG_CUDA(cudaStreamSynchronize(st));
         if ((rc = sliced_error(p))) return rc;
         worst = 0.0;
-        for (int j = 0; j < n; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
+        for (size_t j = 0; j < nn; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
         if (worst <= tol || it >= maxiter) break;
         if ((rc = inner(R, m, D, m))) return rc;
         {

@@ -153,7 +153,9 @@ DPLR_API int dplr_gpu_prepare_mixed(dplr_gpu_plan plan, int slices, void *stream
 DPLR_API int dplr_gpu_prepare_mixed_caps(dplr_gpu_plan plan, int slices, int fp64_capacitance, void *stream);
 
 /* X := A^-1 B refined until max_j ||B_j - A X_j|| / ||B_j|| <= tol; at
- * most maxiter corrections.  flags: DPLR_GPU_RESIDUAL_SLICED selects the
+ * most maxiter corrections.  For a batch plan (dplr_gpu_batch_create) the
+ * maximum runs over every column of every tree, each with its own rows'
+ * norms, so that every matrix of the batch meets tol.  flags: DPLR_GPU_RESIDUAL_SLICED selects the
  * exact-slice residual (as for dplr_gpu_residual); DPLR_GPU_SOLVE_MIXED
  * makes every inner solve the low-precision sweep (needs
  * dplr_gpu_prepare_mixed) instead of the FP64 sweep.  Reports the final relative residual and the number of
