@@ -481,14 +481,25 @@ __global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items, int nite
                                  int nrhs, double *__restrict__ T, long long lo_off)
 {
     const long long E = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (E >= total) return;
-    // the item (binary search by multiplication) and the element within it
-    // (one 32-bit division: rank * nrhs of one item stays below 2^31)
-    int lo = 0, hi = nitems - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((long long)items[mid].rsum * nrhs <= E) lo = mid; else hi = mid - 1;
+    // the item holding the CTA's first element (one binary search per CTA),
+    // then each thread steps forward from it: a CTA's 256 consecutive
+    // elements span one item or a few small ones.  The element within the
+    // item costs one 32-bit division (rank * nrhs of one item stays below
+    // 2^31).
+    __shared__ int first;
+    if (threadIdx.x == 0) {
+        const long long E0 = (long long)blockIdx.x * blockDim.x;
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)items[mid].rsum * nrhs <= E0) lo = mid; else hi = mid - 1;
+        }
+        first = lo;
     }
+    __syncthreads();
+    if (E >= total) return;
+    int lo = first;
+    while (lo + 1 < nitems && (long long)items[lo + 1].rsum * nrhs <= E) ++lo;
     const SReduceItem R = items[lo];
     const long long cnt = (long long)R.rank * nrhs;
     const int e = (int)(E - (long long)R.rsum * nrhs);
@@ -701,6 +712,27 @@ static int sliced_tile_rows(const Plan *p)
     return tc::M;
 }
 
+// The tcgen05 residual also takes leaves and blocks smaller than a tile
+// when each lies inside one 128-row tile (n divides 128, rows aligned to n):
+// they are stored as 128-row tile-blocks whose other rows are zero.
+static bool fits_tile(int n, int row0)
+{
+    if (n % tc::M == 0) return row0 % tc::M == 0;
+    return n % 16 == 0 && tc::M % n == 0 && row0 % n == 0;
+}
+
+static int resid_tile_rows(const Plan *p)
+{
+    const char *env = std::getenv("DPLR_GB300_SLICED_MMA");
+    if (env && env[0] == '1') return ST;
+    if (p->m % tc::M != 0 || p->max_rank > 256) return ST;
+    for (const LeafDesc &L : p->leaves)
+        if (!fits_tile(L.b, L.row0)) return ST;
+    for (const LRDesc &L : p->lr)
+        if (L.rank > 0 && !fits_tile(L.n, L.row0)) return ST;
+    return tc::M;
+}
+
 int ensure_err_flag(Plan *p)
 {
     if (p->tc_err_h) return 0;
@@ -824,7 +856,7 @@ int sliced_build(Plan *p, int ns, cudaStream_t st)
     Sliced *S = new Sliced();
     p->sliced = S;
     S->ns = ns;
-    if (sliced_tile_rows(p) == tc::M) return sliced_build_tb(p, S, st);
+    if (resid_tile_rows(p) == tc::M) return sliced_build_tb(p, S, st);
 
     // layout: V column-major (ld n), U row-major (stride pad8(rank)), leaves row-major
     std::vector<long long> vs_off(p->lr.size()), us_off(p->lr.size()), ds_off(p->leaves.size());
@@ -1568,6 +1600,7 @@ struct RSliceJob {
     long long src;          // column-major rows x cols (ld)
     long long dst;          // tile-block base
     int ld, rows, cols, nkb, exp;
+    int roff = 0;           // tile row of the first row (blocks smaller than a tile)
 };
 
 __device__ __forceinline__ int find_job(const int *base, int njobs, int g)
@@ -1595,10 +1628,11 @@ __global__ void slice_r_tb_kernel(const RSliceJob *jobs, const int *row_base, in
     for (int k = 0; k < J.cols; ++k) mx = fmax(mx, fabs(src[J.src + r + (long long)k * J.ld]));
     const int e = scale_exp(mx);
     exps[J.exp + r] = e;
-    bf16 *base = dst + J.dst + (long long)(r >> 7) * J.nkb * kTbA;
+    const int rr = r + J.roff;
+    bf16 *base = dst + J.dst + (long long)(rr >> 7) * J.nkb * kTbA;
     for (int k = 0; k < J.nkb * 16; ++k) {
         const double v = k < J.cols ? src[J.src + r + (long long)k * J.ld] : 0.0;
-        slice_d<NS>(v, e, base + (long long)(k >> 4) * kTbA + tc2::tbo(r & 127, k & 15), stride);
+        slice_d<NS>(v, e, base + (long long)(k >> 4) * kTbA + tc2::tbo(rr & 127, k & 15), stride);
     }
 }
 
@@ -1976,20 +2010,39 @@ void launch_expand_tb(const Plan *p, const SSchedule &S, const bf16 *apool, long
 }  // namespace
 
 // -------------------------------------------------- exact-slice residual
+// Row exponent of a padding row of a tile-block (a block smaller than the
+// tile): below every real one, so that it never sets a tile's alignment;
+// its rows are zero and add nothing whatever the shift.
+constexpr int kPadExp = -(1 << 20);
+
 static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
 {
+    // Exponent slots: V per rank, U and leaves per row.  A block or leaf of
+    // n < 128 rows gets a whole tile of slots (eu_off / ed_off: the tile's
+    // row 0), its rows at roff = row0 % 128, the others padding.
     std::vector<int> ev_off(p->lr.size()), eu_off(p->lr.size()), ed_off(p->leaves.size());
+    std::vector<std::pair<int, int>> pads;           // [begin, end) of padding slots
     int nexp = 0;
+    auto rows_slots = [&](int n, int row0) {
+        const int base = nexp;
+        if (n % tc2::M == 0) {
+            nexp += n;
+        } else {
+            const int roff = row0 % tc2::M;
+            if (roff > 0) pads.push_back({base, base + roff});
+            if (roff + n < tc2::M) pads.push_back({base + roff + n, base + tc2::M});
+            nexp += tc2::M;
+        }
+        return base;
+    };
     for (size_t b = 0; b < p->lr.size(); ++b) {
         ev_off[b] = nexp;
         nexp += p->lr[b].rank;
-        eu_off[b] = nexp;
-        nexp += p->lr[b].n;
+        eu_off[b] = rows_slots(p->lr[b].n, p->lr[b].row0);
     }
-    for (size_t i = 0; i < p->leaves.size(); ++i) {
-        ed_off[i] = nexp;
-        nexp += p->leaves[i].b;
-    }
+    for (size_t i = 0; i < p->leaves.size(); ++i) ed_off[i] = rows_slots(p->leaves[i].b, p->leaves[i].row0);
+    auto small = [](int n) { return n % tc2::M != 0; };
+    auto roff_of = [&](int n, int row0) { return small(n) ? row0 % tc2::M : 0; };
     VLayout VL;
     std::vector<std::array<long long, 4>> vdst;
     std::vector<std::array<int, 4>> vnr;
@@ -2003,18 +2056,20 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
         const LRDesc &L = p->lr[b];
         if (L.rank == 0) continue;
         const int nkb = (L.rank + 15) / 16;
+        const int ro = roff_of(L.n, L.row0);
         ua[b] = el;
-        el += (long long)(L.n / tc2::M) * nkb * kTbA;
+        el += (long long)std::max(1, L.n / tc2::M) * nkb * kTbA;
         ubase.push_back(nurows);
-        uj.push_back(RSliceJob{L.u, ua[b], L.n, L.n, L.rank, nkb, eu_off[b]});
+        uj.push_back(RSliceJob{L.u, ua[b], L.n, L.n, L.rank, nkb, eu_off[b] + ro, ro});
         nurows += L.n;
     }
     for (size_t i = 0; i < p->leaves.size(); ++i) {
         const LeafDesc &L = p->leaves[i];
+        const int ro = roff_of(L.b, L.row0);
         la[i] = el;
-        el += (long long)(L.b / tc2::M) * (L.b / 16) * kTbA;
+        el += (long long)std::max(1, L.b / tc2::M) * (L.b / 16) * kTbA;
         lbase.push_back(nlrows);
-        lj.push_back(RSliceJob{L.d, la[i], L.b, L.b, L.b, L.b / 16, ed_off[i]});
+        lj.push_back(RSliceJob{L.d, la[i], L.b, L.b, L.b, L.b / 16, ed_off[i] + ro, ro});
         nlrows += L.b;
     }
     S->stride = al32(std::max<long long>(el, 1));
@@ -2024,7 +2079,11 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
     DG_CUDA(cudaMemsetAsync(S->pool, 0, (size_t)kNS * S->stride * sizeof(bf16), st));
     S->nexp = nexp;
     int rc;
-    if ((rc = dev_vec(std::vector<int>(std::max(nexp, 1), 0), &S->exps, &S->bytes))) return rc;
+    {
+        std::vector<int> e0(std::max(nexp, 1), 0);
+        for (const auto &pr : pads) std::fill(e0.begin() + pr.first, e0.begin() + pr.second, kPadExp);
+        if ((rc = dev_vec(e0, &S->exps, &S->bytes))) return rc;
+    }
     {
         VSliceJob *d_vj = nullptr;
         RSliceJob *d_uj = nullptr, *d_lj = nullptr;
@@ -2088,12 +2147,20 @@ static int sliced_build_tb(Plan *p, Sliced *S, cudaStream_t st)
         // each term keeps its own row and column exponents (one read-out per
         // term): sharing them across levels costs the residual about 3x in
         // accuracy on the N = 2^18 kernel matrix
+        if (small(L.n)) {                     // one tile, the block's rows inside it
+            per[L.row0 / tc2::M].push_back(XTerm{ua[b], A.reduces[ridx[b]].tpad, L.rank, eu_off[b], 0, ridx[b]});
+            continue;
+        }
         for (int t0 = L.row0; t0 < L.row0 + L.n; t0 += tc2::M)
             per[t0 / tc2::M].push_back(XTerm{ua[b] + (long long)((t0 - L.row0) / tc2::M) * nkb * kTbA,
                                              A.reduces[ridx[b]].tpad, L.rank, eu_off[b] + (t0 - L.row0), 0, ridx[b]});
     }
     for (size_t i = 0; i < p->leaves.size(); ++i) {
         const LeafDesc &L = p->leaves[i];
+        if (small(L.b)) {
+            per[L.row0 / tc2::M].push_back(XTerm{la[i], L.row0 / 16, L.b, ed_off[i], 1, -1});
+            continue;
+        }
         for (int t0 = L.row0; t0 < L.row0 + L.b; t0 += tc2::M)
             per[t0 / tc2::M].push_back(XTerm{la[i] + (long long)((t0 - L.row0) / tc2::M) * (L.b / 16) * kTbA,
                                              L.row0 / 16, L.b, ed_off[i] + (t0 - L.row0), 1, -1});

@@ -21,16 +21,28 @@ int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double 
                  cudaStream_t st);
 long long factor_bytes(const Plan *p);
 
-// Column 2-norms of an m x n matrix (one CTA per column).
-__global__ void colnorm_kernel(const double *A, int m, int lda, double *out)
+// Column 2-norms of an m x n matrix: one CTA of kNormThreads per column,
+// four independent sums per thread so that four loads are in flight (one
+// CTA per SM pair covers a 256-column block in one wave).
+constexpr int kNormThreads = 1024;
+
+__global__ void __launch_bounds__(kNormThreads) colnorm_kernel(const double *A, int m, int lda, double *out)
 {
-    __shared__ double red[256];
+    __shared__ double red[kNormThreads];
     const double *a = A + (long long)blockIdx.x * lda;
-    double s = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) s = fma(a[i], a[i], s);
-    red[threadIdx.x] = s;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = threadIdx.x;
+    for (; i + 3 * kNormThreads < m; i += 4 * kNormThreads) {
+        const double x0 = a[i], x1 = a[i + kNormThreads], x2 = a[i + 2 * kNormThreads], x3 = a[i + 3 * kNormThreads];
+        s0 = fma(x0, x0, s0);
+        s1 = fma(x1, x1, s1);
+        s2 = fma(x2, x2, s2);
+        s3 = fma(x3, x3, s3);
+    }
+    for (; i < m; i += kNormThreads) s0 = fma(a[i], a[i], s0);
+    red[threadIdx.x] = (s0 + s1) + (s2 + s3);
     __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    for (int k = kNormThreads / 2; k > 0; k >>= 1) {
         if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
         __syncthreads();
     }
@@ -114,7 +126,7 @@ int refine_fixed(Plan *p, int n, const double *B, int ldb, double *X, int ldx, i
 int colnorms_device(const double *A, int m, int n, int lda, double *out, cudaStream_t st)
 {
     if (n <= 0) return 0;
-    colnorm_kernel<<<n, 256, 0, st>>>(A, m, lda, out);
+    colnorm_kernel<<<n, kNormThreads, 0, st>>>(A, m, lda, out);
     note_launch();
     DG_CUDA(cudaGetLastError());
     return 0;

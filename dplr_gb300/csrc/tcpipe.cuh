@@ -508,6 +508,8 @@ __global__ void __maxnreg__(kRegs)
                         break;
                     }
                     fence_after();
+                    // (every warp reads: skipping the columns past nrhs here
+                    // made the full-width inner-solve expand 7 % slower)
 #pragma unroll
                     for (int c4 = 0; c4 < C4N; ++c4) {
                         long long W[4];
@@ -595,14 +597,16 @@ __global__ void __maxnreg__(kRegs)
                         break;
                     }
                     fence_after();
+                    if (j0 < nrhs) {             // warps past the last column only release
 #pragma unroll
-                    for (int c4 = 0; c4 < C4N; ++c4) {
-                        __int128 W[4];
-                        read4<D>(trow, c4, W);
+                        for (int c4 = 0; c4 < C4N; ++c4) {
+                            __int128 W[4];
+                            read4<D>(trow, c4, W);
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const int sh = rdel + __shfl_sync(0xffffffffu, cdl, c4 * 4 + u);
-                            acc[c4 * 4 + u] += ashift(W[u], sh);
+                            for (int u = 0; u < 4; ++u) {
+                                const int sh = rdel + __shfl_sync(0xffffffffu, cdl, c4 * 4 + u);
+                                acc[c4 * 4 + u] += ashift(W[u], sh);
+                            }
                         }
                     }
                     fence_before();
@@ -726,6 +730,9 @@ __global__ void __maxnreg__(kRegs)
             const PItem itm = items[u / njp];
             const int jp = u % njp;
             const int ncol = min(itm.nr, itm.rank - itm.kt);     // live ranks of the tile
+            // warps whose right-hand sides or rank columns are all past the
+            // live ones only release tensor memory
+            const bool live = jp * M + lq * 32 < nrhs && ch * CPW < ncol;
             __int128 acc[CPW];
 #pragma unroll
             for (int c = 0; c < CPW; ++c) acc[c] = 0;
@@ -738,12 +745,14 @@ __global__ void __maxnreg__(kRegs)
                 fence_after();
                 // columns past the tile's padded rank hold stale values; they
                 // are read (the loads are warp-collective) but never written
+                if (live) {
 #pragma unroll
-                for (int c4 = 0; c4 < C4N; ++c4) {
-                    __int128 W[4];
-                    read4<D>(trow, c4, W);
+                    for (int c4 = 0; c4 < C4N; ++c4) {
+                        __int128 W[4];
+                        read4<D>(trow, c4, W);
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) acc[c4 * 4 + v] += W[v];
+                        for (int v = 0; v < 4; ++v) acc[c4 * 4 + v] += W[v];
+                    }
                 }
                 fence_before();
                 __syncwarp();

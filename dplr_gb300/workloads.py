@@ -319,7 +319,8 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
                    "refined_solve_exact_residual": {
                        "ms": exact_ms, "max_rel_resid": exact_worst, "kernels": exact_kernels,
                        "note": "the same refined-solve graphs with exact-slice residuals in the corrections "
-                               "(mma.sync kernels for these leaf-64 matrices)"},
+                               "(tcgen05 kernels; the 64-row leaves and blocks are stored as half-empty "
+                               "128-row tiles)"},
                    "kernels_ms": kern,
                    "setup_s": {"generate": t_gen, "upload": t_up, "factor": t_fac}},
     }

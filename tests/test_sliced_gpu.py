@@ -133,7 +133,8 @@ def test_mixed_refined_solve_reaches_1e12(shape):
 
 def _plan(t, mma: bool, mixed_slices: int = 0):
     """Plan whose sliced products run on the mma.sync kernels (mma=True) or
-    on the tcgen05 kernels (128-row tiles; leaves must be multiples of 128)."""
+    on the tcgen05 kernels (128-row tiles; leaves that are multiples of 128
+    rows, or whose size divides 128 for the residual)."""
     import os
     from dplr_gb300.plan import GpuPlan
     old = os.environ.get("DPLR_GB300_SLICED_MMA")
@@ -152,16 +153,20 @@ def _plan(t, mma: bool, mixed_slices: int = 0):
     return p
 
 
-@pytest.mark.parametrize("kind", ["random_rank160", "kernel2d"])
+@pytest.mark.parametrize("kind", ["random_rank160", "kernel2d", "leaf64_rank4"])
 def test_tcgen05_residual_matches_mma_sync(kind):
     """Both kernel families compute exact integer products of 57-bit slices
     and round once; their operand slicing differs (the tcgen05 path cuts U
     and T per 128-row tile-block), so the two agree to the slice-truncation
     level, about 2^-57 |A||x|.  70 right-hand sides exercise a ragged
-    64-column tile; ranks above 128 exercise the panel's later rank tiles."""
+    64-column tile; ranks above 128 exercise the panel's later rank tiles;
+    64-row leaves and blocks (stored as half-empty 128-row tiles) with ranks
+    1-4 exercise the small-block layout."""
     from dplr_gb300 import gen_gpu
     if kind == "kernel2d":
         t = gen_gpu.kernel_tree_2d(n=8192, leaf=128, rmax=96, seed=8)
+    elif kind == "leaf64_rank4":
+        t = gen.random_tree(2048, 64, [4, 1, 3, 2, 4], seed=11)
     else:
         t = gen.random_tree(2048, 128, [160, 140, 100, 40], seed=9)
     rng = np.random.default_rng(10)
@@ -244,3 +249,41 @@ def test_tensor_core_capacitance_matches_fp64():
     assert rt <= 1e-12 and rf <= 1e-12, (rt, rf)
     assert float(((xt - xf).norm(dim=1) / xf.norm(dim=1)).max()) <= 1e-9
     assert r0t <= 4 * r0f and r0f <= 4 * r0t, (r0t, r0f)
+
+
+def test_tcgen05_residual_of_a_small_block_batch():
+    """A batch of leaf-64, rank <= 4 trees (as the 512-matrix workload) on
+    the tcgen05 residual: every matrix's rows against the exact residual of
+    its own tree, and against the mma.sync kernels."""
+    import os
+    from dplr_gb300.plan import GpuPlan
+    trees = [gen.random_tree(1024, 64, [2, 4, 1, 3], seed=21), gen.random_tree(2048, 64, [1, 1, 4, 2, 3], seed=22),
+             gen.random_tree(1024, 64, [3, 0, 2, 1], seed=23)]
+    rng = np.random.default_rng(24)
+    m = sum(t.size for t in trees)
+    x = rng.standard_normal((5, m))
+    b = rng.standard_normal((5, m))
+    out = {}
+    for mma in (False, True):
+        old = os.environ.get("DPLR_GB300_SLICED_MMA")
+        os.environ["DPLR_GB300_SLICED_MMA"] = "1" if mma else "0"
+        try:
+            p = GpuPlan.batch(trees)
+            p.prepare_sliced()
+        finally:
+            if old is None:
+                del os.environ["DPLR_GB300_SLICED_MMA"]
+            else:
+                os.environ["DPLR_GB300_SLICED_MMA"] = old
+        out[mma] = p.residual(torch.tensor(x, device="cuda"), torch.tensor(b, device="cuda"),
+                              precise=True).cpu().numpy()
+        p.close()
+    o = 0
+    for t in trees:
+        n = t.size
+        want = exact_residual(t, x[:, o:o + n], b[:, o:o + n])
+        nax = float(np.linalg.norm((b[:, o:o + n] - want).astype(np.float64)))
+        for mma in (False, True):
+            err = float(np.linalg.norm((out[mma][:, o:o + n] - want).astype(np.float64))) / nax
+            assert err <= 1e-15, (mma, err)
+        o += n
