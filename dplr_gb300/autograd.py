@@ -30,8 +30,8 @@ def _sync_pool(plan: GpuPlan, pool: torch.Tensor, factor: bool) -> None:
     if getattr(plan, "_pool_key", None) != key:
         plan.write_pool(pool.detach())
         plan._pool_key = key
-    if factor and not (plan.factored and plan.factored_transposed):
-        plan.factor(transposed=True)
+    if factor and not plan.factored:
+        plan.factor()
 
 
 class _PlrApply(torch.autograd.Function):

@@ -8,9 +8,13 @@
 //   Z  = D^-1 W          (panels Z1 = A1^-1 U1, Z2 = A2^-1 U2)
 //   K  = I + S V~^T Z = [[I, S1 V1^T Z2], [S2 V2^T Z1, I]]
 //   A^-1 b = z - Z K^-1 S V~^T z,       z = D^-1 b
-//   A^-T b = z - Zt S K^-T W^T z,       z = D^-T b,  Zt = D^-T V~
-// (Zt holds Zt1 = A2^-T V1, Zt2 = A1^-T V2, needed only for transposed
-// solves and for the explicit inverse).
+// Its transpose A^-T = D^-T (I - V~ S K^-T Z^T) reuses the same factors:
+// the transposed solve sweeps top-down, g -= V~ S K^-T Z^T g per level
+// (root first, every node of a level at once), then applies the leaf
+// inverses transposed; nothing per level is stored.  The explicit inverse
+// also needs Zt = D^-T V~ (Zt1 = A2^-T V1, Zt2 = A1^-T V2, built with
+// DPLR_GPU_FACTOR_TRANSPOSED by the same top-down sweep truncated to the
+// deeper levels).
 //
 // Device layout: per H level l one m x r_l matrix Z_l (ld m; rows of the
 // ne block of node p hold Z1(p), rows of its sw block hold Z2(p)), the
@@ -225,9 +229,12 @@ static int ensure_work(Fact *F, const Plan *p, int nrhs)
     return ensure_buffer(&F->work, &F->work_doubles, need);
 }
 
-// One bottom-up sweep: leaves, then H levels from the deepest down to
-// `lowest`.  op N: Xo = D^-1-style solve of B; op T: the transposed solve.
-// B and Xo are m x nrhs (ld ldb / ldx) and must not alias.
+// One sweep over the leaves and the H levels from `lowest` to the deepest
+// (all of them for lowest = 0).  op N, bottom-up: Xo = leaf^-1 B, then per
+// level from the deepest up: Xo -= Z K^-1 S V~^T Xo.  op T, top-down: a
+// copy G of B takes G -= V~ S K^-T Z^T G per level from `lowest` down to
+// the deepest, then Xo = leaf^-T G.  B and Xo are m x nrhs (ld ldb / ldx)
+// and must not alias.
 static int sweep(Plan *p, Fact *F, int trans, int lowest, const double *B, int ldb, double *Xo,
                  int ldx, int nrhs, cudaStream_t st)
 {
@@ -236,24 +243,32 @@ static int sweep(Plan *p, Fact *F, int trans, int lowest, const double *B, int l
     double *T = F->work;
     double *W = F->work + (size_t)p->total_rank * nrhs;
     double *partials = W + (size_t)p->total_rank * nrhs;
-    const Schedule &leaf = trans ? F->leafT : F->leafN;
-    if ((rc = run_expand(leaf, F->leafinv, nullptr, B, ldb, Xo, ldx, nrhs, 1.0, 0.0, st))) return rc;
-    for (int l = (int)F->lv.size() - 1; l >= lowest; --l) {
-        const LevelOps &L = F->lv[l];
-        if (L.width == 0) continue;
-        if (!trans) {
+    if (!trans) {
+        if ((rc = run_expand(F->leafN, F->leafinv, nullptr, B, ldb, Xo, ldx, nrhs, 1.0, 0.0, st))) return rc;
+        for (int l = (int)F->lv.size() - 1; l >= lowest; --l) {
+            const LevelOps &L = F->lv[l];
+            if (L.width == 0) continue;
             if ((rc = run_panel(L.n, p->pool, Xo, ldx, nrhs, partials, st))) return rc;
             if ((rc = run_reduce(L.n, p->pool, partials, nrhs, T, st))) return rc;
             if ((rc = run_caps(L.n, F->kpool, nullptr, 0, T, W, nrhs, st))) return rc;
             if ((rc = run_expand(L.n, F->zpool, W, nullptr, 0, Xo, ldx, nrhs, -1.0, 1.0, st))) return rc;
-        } else {
-            if ((rc = run_panel(L.t, p->pool, Xo, ldx, nrhs, partials, st))) return rc;
-            if ((rc = run_reduce(L.t, nullptr, partials, nrhs, T, st))) return rc;
-            if ((rc = run_caps(L.t, F->kpool, p->pool, 1, T, W, nrhs, st))) return rc;
-            if ((rc = run_expand(L.t, F->ztpool, W, nullptr, 0, Xo, ldx, nrhs, -1.0, 1.0, st))) return rc;
         }
+        return 0;
     }
-    return 0;
+    const int m = p->m;
+    if ((rc = ensure_buffer(&F->gtr, &F->gtr_doubles, (size_t)m * nrhs))) return rc;
+    double *G = F->gtr;
+    DG_CUDA(cudaMemcpy2DAsync(G, (size_t)m * sizeof(double), B, (size_t)ldb * sizeof(double),
+                              (size_t)m * sizeof(double), nrhs, cudaMemcpyDeviceToDevice, st));
+    for (int l = lowest; l < (int)F->lv.size(); ++l) {
+        const LevelOps &L = F->lv[l];
+        if (L.width == 0) continue;
+        if ((rc = run_panel(L.t, F->zpool, G, m, nrhs, partials, st))) return rc;       // Z^T G
+        if ((rc = run_reduce(L.t, nullptr, partials, nrhs, T, st))) return rc;
+        if ((rc = run_caps(L.t, F->kpool, p->pool, 1, T, W, nrhs, st))) return rc;     // S K^-T
+        if ((rc = run_expand(L.t, p->pool, W, nullptr, 0, G, m, nrhs, -1.0, 1.0, st))) return rc;   // V~
+    }
+    return run_expand(F->leafT, F->leafinv, nullptr, G, m, Xo, ldx, nrhs, 1.0, 0.0, st);
 }
 
 // ------------------------------------------------------------- schedules
@@ -280,9 +295,9 @@ static void build_level_schedules(Plan *p, Fact *F)
                         it.f = D.v;
                         it.n = D.n;
                         it.in0 = D.col0;
-                    } else {               // U_b^T x[row0 rows]
-                        it.f = D.u;
-                        it.n = D.n;
+                    } else {               // Z_l[row0 rows]^T g[row0 rows] (Z_l: ld m, in zpool)
+                        it.f = F->zoff[l] + D.row0;
+                        it.n = m;
                         it.in0 = D.row0;
                     }
                     it.p = poff;
@@ -300,14 +315,15 @@ static void build_level_schedules(Plan *p, Fact *F)
                 r.nch = nch;
                 S.reduces.push_back(r);
                 poff += (long long)nch * D.rank;
-                // update tiles: rows of the block (op N: U side, with Z_l);
-                // op T: columns of the block (V side, with Zt_l)
+                // update tiles: op N, rows of the block with Z_l (ld m, in
+                // zpool); op T, the block's column rows with its V (ld n,
+                // in the factor pool)
                 int out0 = trans ? D.col0 : D.row0;
                 for (int t0 = out0; t0 < out0 + D.n; t0 += R) {
                     TileTerm tt;
-                    tt.a = F->zoff[l] + t0;
+                    tt.a = trans ? D.v + (t0 - D.col0) : F->zoff[l] + t0;
                     tt.b = D.toff;
-                    tt.lda = m;
+                    tt.lda = trans ? D.n : m;
                     tt.K = D.rank;
                     tt.trans_a = 0;
                     tt.src = 0;
@@ -386,6 +402,7 @@ void factor_free(Plan *p)
     cudaFree(F->d_leafsize);
     cudaFree(F->d_info);
     cudaFree(F->work);
+    cudaFree(F->gtr);
     cudaFree(F->rhs);
     cudaFree(F->vec);
     delete F;
@@ -563,8 +580,6 @@ int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double 
 {
     Fact *F = (Fact *)p->fact;
     if (!F) return fail(DPLR_GPU_ESTATE, "solve: plan is not factored");
-    if (trans && !F->transposed)
-        return fail(DPLR_GPU_ESTATE, "solve: factorisation was built without transposed panels");
     if (nrhs <= 0 || p->m == 0) return 0;
     return sweep(p, F, trans, 0, B, ldb, X, ldx, nrhs, st);
 }
@@ -573,7 +588,7 @@ long long factor_bytes(const Plan *p)
 {
     const Fact *F = (const Fact *)p->fact;
     if (!F) return 0;
-    return F->bytes + (long long)(F->work_doubles + F->rhs_doubles + F->vec_doubles) * 8;
+    return F->bytes + (long long)(F->work_doubles + F->rhs_doubles + F->vec_doubles + F->gtr_doubles) * 8;
 }
 
 }  // namespace dg

@@ -8,7 +8,7 @@ namespace dg {
 
 struct LevelOps {
     Schedule n;       // op N: panels on V, caps K^-1, updates with Z_l
-    Schedule t;       // op T: panels on U, caps K^-T scaled, updates with Zt_l
+    Schedule t;       // op T: panels on Z_l, caps S K^-T, updates with V
     int width = 0;    // r_l
     std::vector<int> blocks;   // LRDesc indices at this level
     std::vector<int> nodes;    // HDesc indices at this level
@@ -38,6 +38,8 @@ struct Fact {
     size_t rhs_doubles = 0;
     double *vec = nullptr;            // refinement vectors
     size_t vec_doubles = 0;
+    double *gtr = nullptr;            // the transposed sweep's running right-hand side
+    size_t gtr_doubles = 0;
     long long bytes = 0;
     // first singular matrix met while factoring: 0 none, 1 leaf, 2 capacitance
     int sing_kind = 0, sing_index = -1, sing_info = 0;

@@ -112,8 +112,10 @@ DPLR_API void dplr_gpu_set_recompress(double eps);
 /* Woodbury factorisation of the planned matrix (replaces forming inv(A)
  * with DPLR's dplrgeinv, src/dplrinv.c:93, when the goal is solving):
  * leaf inverses, per-level panels Z = D^-1 W and capacitance inverses
- * (I + S V~^T Z)^-1, all FP64.  DPLR_GPU_FACTOR_TRANSPOSED also builds
- * the panels D^-T V~ needed by transposed solves. */
+ * (I + S V~^T Z)^-1, all FP64.  Transposed solves reuse these factors
+ * (A^-T = D^-T (I - V~ S K^-T Z^T), swept top-down).
+ * DPLR_GPU_FACTOR_TRANSPOSED also builds the panels D^-T V~, which only
+ * the explicit inverse (dplrgeinv on the device) needs. */
 #define DPLR_GPU_FACTOR_TRANSPOSED 1
 DPLR_API int dplr_gpu_factor(dplr_gpu_plan plan, int flags, void *stream);
 DPLR_API long long dplr_gpu_factor_device_bytes(dplr_gpu_plan plan);

@@ -42,7 +42,7 @@ def test_solve_matches_dense(name, trans):
     t = CASES[name]()
     m = t.size
     p = GpuPlan(t)
-    p.factor(transposed=True)
+    p.factor()          # the transposed solve reuses the forward factors
     rng = np.random.default_rng(5)
     b = rng.standard_normal((7, m))
     x = p.solve(torch.tensor(b, device="cuda"), trans=trans).cpu().numpy()
