@@ -130,6 +130,132 @@ __global__ void __launch_bounds__(256) lu_inverse_kernel(double *base, const lon
     if (tid == 0) info[id] = 0;
 }
 
+// The same inverse with the matrix in shared memory, for n <= kSmemInvMax
+// (at most 206 KB): the LU is the same right-looking elimination, in the
+// same order, as lu_inverse_kernel's; the inverse follows LAPACK dgetri's
+// unblocked algorithm -- inv(U) in place column by column (dtrti2), then
+// inv(A) = inv(U) inv(L) column by column from the last, then the pivots'
+// column interchanges in reverse order -- with each column's dot products
+// split over the threads.  The matrix goes back to global memory once.
+constexpr int kSmemInvMax = 160;
+
+__global__ void __launch_bounds__(256) lu_inverse_smem_kernel(double *base, const long long *off,
+                                                              const int *size, int *info)
+{
+    extern __shared__ double S[];        // n x n (ld n), then n doubles of work
+    __shared__ int piv[kSmemInvMax];
+    __shared__ double rv[256];
+    __shared__ int ri[256];
+    __shared__ int singular;
+    const int id = blockIdx.x, tid = threadIdx.x, bs = blockDim.x;
+    double *A = base + off[id];
+    const int n = size[id];
+    double *wk = S + n * n;
+    for (int e = tid; e < n * n; e += bs) S[e] = A[e];
+    if (tid == 0) singular = 0;
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        double best = -1.0;
+        int bi = j;
+        for (int i = j + tid; i < n; i += bs) {
+            const double v = fabs(S[i + j * n]);
+            if (v > best) { best = v; bi = i; }
+        }
+        rv[tid] = best;
+        ri[tid] = bi;
+        __syncthreads();
+        for (int s = bs / 2; s > 0; s >>= 1) {
+            if (tid < s) {
+                const double o = rv[tid + s];
+                const int oi = ri[tid + s];
+                if (o > rv[tid] || (o == rv[tid] && oi < ri[tid])) { rv[tid] = o; ri[tid] = oi; }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            piv[j] = ri[0];
+            if (rv[0] == 0.0 && singular == 0) singular = j + 1;
+        }
+        __syncthreads();
+        const int p = piv[j];
+        if (p != j)
+            for (int c = tid; c < n; c += bs) {
+                const double t = S[j + c * n];
+                S[j + c * n] = S[p + c * n];
+                S[p + c * n] = t;
+            }
+        __syncthreads();
+        const double d = S[j + j * n];
+        if (d != 0.0) {
+            const double inv = 1.0 / d;
+            for (int i = j + 1 + tid; i < n; i += bs) S[i + j * n] *= inv;
+        }
+        __syncthreads();
+        const int w = n - j - 1;
+        for (int e = tid; e < w * w; e += bs) {
+            const int i = j + 1 + e % w, c = j + 1 + e / w;
+            S[i + c * n] -= S[i + j * n] * S[j + c * n];
+        }
+        __syncthreads();
+    }
+    if (singular) {
+        if (tid == 0) info[id] = singular;
+        return;
+    }
+    // inv(U) in place: column j = -inv(U)[0:j, 0:j] U[0:j, j] / U[j, j]
+    for (int j = 0; j < n; ++j) {
+        for (int i = tid; i < j; i += bs) wk[i] = S[i + j * n];
+        __syncthreads();
+        const double ujj = 1.0 / S[j + j * n];
+        for (int i = tid; i < j; i += bs) {
+            double t = 0.0;
+            for (int k = i; k < j; ++k) t = fma(S[i + k * n], wk[k], t);
+            S[i + j * n] = -ujj * t;
+        }
+        __syncthreads();
+        if (tid == 0) S[j + j * n] = ujj;
+        __syncthreads();
+    }
+    // inv(A) inv(P)^T-free part: column j -= columns j+1.. times L's column j
+    for (int j = n - 2; j >= 0; --j) {
+        for (int i = j + 1 + tid; i < n; i += bs) {
+            wk[i] = S[i + j * n];
+            S[i + j * n] = 0.0;
+        }
+        __syncthreads();
+        for (int r = tid; r < n; r += bs) {
+            double t = S[r + j * n];
+            for (int k = j + 1; k < n; ++k) t = fma(-S[r + k * n], wk[k], t);
+            S[r + j * n] = t;
+        }
+        __syncthreads();
+    }
+    // the row interchanges of the LU become column interchanges
+    for (int j = n - 2; j >= 0; --j) {
+        const int p = piv[j];
+        if (p != j)
+            for (int r = tid; r < n; r += bs) {
+                const double t = S[r + j * n];
+                S[r + j * n] = S[r + p * n];
+                S[r + p * n] = t;
+            }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * n; e += bs) A[e] = S[e];
+    if (tid == 0) info[id] = 0;
+}
+
+// Copy of every leaf into the inverse pool: one CTA per leaf.
+__global__ void copy_leaves_kernel(const LeafDesc *__restrict__ leaves, const double *__restrict__ pool,
+                                   const long long *__restrict__ dst_off, double *__restrict__ dst)
+{
+    const LeafDesc L = leaves[blockIdx.x];
+    const double *src = pool + L.d;
+    double *out = dst + dst_off[blockIdx.x];
+    const long long cnt = (long long)L.b * L.b;
+    for (long long e = threadIdx.x; e < cnt; e += blockDim.x) out[e] = src[e];
+}
+
 // Place one factor per block into the rows of a level right-hand side:
 // dst[row0 + i, k] = src[i + k*n] for i < n, k < rank (ld of dst = m).
 struct ScatterItem {
@@ -193,30 +319,28 @@ static int zero_device(double *p, long long n, cudaStream_t st)
     return 0;
 }
 
-static int batched_inverse(double *base, long long *d_off, int *d_size, int count, int *d_info,
-                           long long span, cudaStream_t st, const char *what, Fact *F = nullptr,
-                           int kind = 0, const std::vector<int> *ids = nullptr)
+// Inverts `count` matrices (offsets d_off, orders d_size; nmax the largest,
+// host side) and writes each one's info to d_info[i]; asynchronous: the
+// caller reads the infos back once the whole factorisation has run.  Up to
+// kSmemInvMax the matrices are inverted in shared memory, else in place in
+// global memory with a scratch of `span` doubles (freed in stream order).
+static int batched_inverse(double *base, long long *d_off, int *d_size, int count, int nmax, int *d_info,
+                           long long span, cudaStream_t st)
 {
     if (count == 0) return 0;
-    double *work = nullptr;
-    DG_ALLOC(&work, std::max<long long>(span, 1) * sizeof(double));
-    lu_inverse_kernel<<<count, 256, 0, st>>>(base, d_off, d_size, work, d_info);
+    if (nmax <= kSmemInvMax) {
+        const int smem = (nmax * nmax + nmax) * (int)sizeof(double);
+        DG_CUDA(cudaFuncSetAttribute(lu_inverse_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        lu_inverse_smem_kernel<<<count, 256, smem, st>>>(base, d_off, d_size, d_info);
+    } else {
+        double *work = nullptr;
+        if (cudaMallocAsync((void **)&work, std::max<long long>(span, 1) * sizeof(double), st) != cudaSuccess)
+            return fail(DPLR_GPU_ENOMEM, "inverse: cannot allocate %lld doubles of scratch", span);
+        lu_inverse_kernel<<<count, 256, 0, st>>>(base, d_off, d_size, work, d_info);
+        cudaFreeAsync(work, st);
+    }
     note_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(work);
-    if (e != cudaSuccess) return fail(DPLR_GPU_ECUDA, "%s inverse: %s", what, cudaGetErrorString(e));
-    std::vector<int> info(count);
-    DG_CUDA(cudaMemcpy(info.data(), d_info, count * sizeof(int), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < count; ++i)
-        if (info[i] != 0) {
-            if (F) {
-                F->sing_kind = kind;
-                F->sing_index = ids ? (*ids)[i] : i;
-                F->sing_info = info[i];
-            }
-            return fail(DPLR_GPU_ESINGULAR, "%s %d is singular (zero pivot %d)", what, i, info[i]);
-        }
+    DG_CUDA(cudaGetLastError());
     return 0;
 }
 
@@ -401,6 +525,9 @@ void factor_free(Plan *p)
     cudaFree(F->d_ksize);
     cudaFree(F->d_leafsize);
     cudaFree(F->d_info);
+    cudaFree(F->d_scat);
+    cudaFree(F->d_inv_off);
+    cudaFree(F->d_inv_size);
     cudaFree(F->work);
     cudaFree(F->gtr);
     cudaFree(F->rhs);
@@ -413,45 +540,28 @@ void factor_free(Plan *p)
 // block at level l placed at the block's rows (U: row0, V: col0).
 static int level_rhs(Plan *p, Fact *F, int l, int which, cudaStream_t st)
 {
-    const LevelOps &L = F->lv[l];
-    const int width = L.width;
+    const int width = F->lv[l].width;
     int rc;
-    if ((rc = ensure_buffer(&F->rhs, &F->rhs_doubles, (size_t)p->m * width))) return rc;
     if ((rc = zero_device(F->rhs, (long long)p->m * width, st))) return rc;
-    std::vector<ScatterItem> items;
-    int maxcnt = 0;
-    for (int b : L.blocks) {
-        const LRDesc &D = p->lr[b];
-        if (D.rank == 0) continue;
-        ScatterItem it;
-        it.src = which == 0 ? D.u : D.v;
-        it.row0 = which == 0 ? D.row0 : D.col0;
-        it.n = D.n;
-        it.rank = D.rank;
-        items.push_back(it);
-        maxcnt = std::max(maxcnt, D.n * D.rank);
-    }
-    if (items.empty()) return 0;
-    ScatterItem *d_items = nullptr;
-    long long dummy = 0;
-    if ((rc = to_device(items, &d_items, &dummy))) return rc;
-    dim3 g((unsigned)std::min(64, (maxcnt + 255) / 256), (unsigned)items.size());
-    scatter_kernel<<<g, 256, 0, st>>>(d_items, p->pool, F->rhs, p->m);
+    const int cnt = F->scat_count[which][l];
+    if (cnt == 0) return 0;
+    dim3 g((unsigned)std::min(64, (F->scat_max[which][l] + 255) / 256), (unsigned)cnt);
+    scatter_kernel<<<g, 256, 0, st>>>(F->d_scat + F->scat_begin[which][l], p->pool, F->rhs, p->m);
     note_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_items);
-    if (e != cudaSuccess) return fail(DPLR_GPU_ECUDA, "level rhs: %s", cudaGetErrorString(e));
+    DG_CUDA(cudaGetLastError());
     return 0;
 }
 
-int factor_build(Plan *p, int flags, cudaStream_t st)
+// Everything of a factorisation that depends on the plan's structure only:
+// offsets, device pools, the level schedules, the levels' scatter items and
+// capacitance inverse lists.  Built once; refactorisations after a change
+// of the values (the adjoint's every step) reuse it.
+static int factor_layout(Plan *p, Fact *F, int flags)
 {
-    factor_free(p);
-    Fact *F = new Fact();
-    p->fact = F;
     F->flags = flags;
     F->transposed = (flags & 1) != 0;
+    F->key_chunk = p->chunk_rows;
+    F->key_nb = p->nb_cap;
     const int nlev = p->levels;
     F->lv.resize(nlev);
     for (size_t b = 0; b < p->lr.size(); ++b) {
@@ -462,9 +572,11 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
     }
     for (size_t nd = 0; nd < p->nodes.size(); ++nd) F->lv[p->nodes[nd].level].nodes.push_back((int)nd);
     long long z = 0;
+    int wmax = 1;
     for (int l = 0; l < nlev; ++l) {
         F->zoff.push_back(z);
         z += align32((long long)p->m * F->lv[l].width);
+        wmax = std::max(wmax, F->lv[l].width);
     }
     F->zdoubles = z;
     std::vector<int> ksize(p->nodes.size());
@@ -505,7 +617,8 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
         (rc = to_device(F->leafoff, &F->d_leafoff, &F->bytes)) ||
         (rc = to_device(lsize, &F->d_leafsize, &F->bytes)))
         return rc;
-    std::vector<int> zeros(std::max(p->nodes.size(), p->leaves.size()) + 1, 0);
+    // one info slot per leaf, then one per node (each inverse writes its own)
+    std::vector<int> zeros(p->leaves.size() + p->nodes.size() + 1, 0);
     if ((rc = to_device(zeros, &F->d_info, &F->bytes))) return rc;
 
     build_level_schedules(p, F);
@@ -515,14 +628,124 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
     if ((rc = upload_schedule(F->leafN, &F->bytes)) || (rc = upload_schedule(F->leafT, &F->bytes)))
         return rc;
 
-    // Leaf inverses.
-    for (size_t i = 0; i < p->leaves.size(); ++i) {
-        const LeafDesc &Lf = p->leaves[i];
-        DG_CUDA(cudaMemcpyAsync(F->leafinv + F->leafoff[i], p->pool + Lf.d,
-                                sizeof(double) * Lf.b * Lf.b, cudaMemcpyDeviceToDevice, st));
+    // scatter items of every level (U, and V for the transposed panels)
+    std::vector<ScatterItem> scat;
+    for (int which = 0; which < 2; ++which) {
+        F->scat_begin[which].assign(nlev, 0);
+        F->scat_count[which].assign(nlev, 0);
+        F->scat_max[which].assign(nlev, 0);
+        for (int l = 0; l < nlev; ++l) {
+            F->scat_begin[which][l] = (int)scat.size();
+            for (int b : F->lv[l].blocks) {
+                const LRDesc &D = p->lr[b];
+                if (D.rank == 0) continue;
+                ScatterItem it;
+                it.src = which == 0 ? D.u : D.v;
+                it.row0 = which == 0 ? D.row0 : D.col0;
+                it.n = D.n;
+                it.rank = D.rank;
+                scat.push_back(it);
+                F->scat_max[which][l] = std::max(F->scat_max[which][l], D.n * D.rank);
+            }
+            F->scat_count[which][l] = (int)scat.size() - F->scat_begin[which][l];
+        }
     }
-    if ((rc = batched_inverse(F->leafinv, F->d_leafoff, F->d_leafsize, (int)p->leaves.size(),
-                              F->d_info, F->leafdoubles, st, "leaf", F, 1)))
+    if ((rc = to_device(scat, &F->d_scat, &F->bytes))) return rc;
+    // capacitance inverses of every level
+    std::vector<long long> ioff;
+    std::vector<int> isize;
+    F->inv_begin.assign(nlev, 0);
+    F->inv_count.assign(nlev, 0);
+    F->inv_max.assign(nlev, 0);
+    for (int l = 0; l < nlev; ++l) {
+        F->inv_begin[l] = (int)ioff.size();
+        for (int nd : F->lv[l].nodes) {
+            const HDesc &H = p->nodes[nd];
+            int r = p->lr[H.ne].rank + p->lr[H.sw].rank;
+            if (r == 0) continue;
+            ioff.push_back(F->koff[nd]);
+            isize.push_back(r);
+            F->inv_ids.push_back(nd);
+            F->inv_max[l] = std::max(F->inv_max[l], r);
+        }
+        F->inv_count[l] = (int)ioff.size() - F->inv_begin[l];
+    }
+    if ((rc = to_device(ioff, &F->d_inv_off, &F->bytes)) || (rc = to_device(isize, &F->d_inv_size, &F->bytes)))
+        return rc;
+    // scratch for the widest level, so that the numeric pass allocates nothing
+    if ((rc = ensure_buffer(&F->rhs, &F->rhs_doubles, (size_t)p->m * wmax))) return rc;
+    return ensure_work(F, p, wmax);
+}
+
+// The first nonzero info of the last numeric pass (leaves first, then the
+// nodes in factorisation order), reported as DPLR does.
+static int factor_check(Plan *p, Fact *F)
+{
+    const size_t nl = p->leaves.size();
+    std::vector<int> info(nl + F->inv_ids.size());
+    if (!info.empty())
+        DG_CUDA(cudaMemcpy(info.data(), F->d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nl; ++i)
+        if (info[i] != 0) {
+            F->sing_kind = 1;
+            F->sing_index = (int)i;
+            F->sing_info = info[i];
+            return fail(DPLR_GPU_ESINGULAR, "leaf %d is singular (zero pivot %d)", (int)i, info[i]);
+        }
+    for (int l = (int)F->lv.size() - 1; l >= 0; --l)
+        for (int q = F->inv_begin[l]; q < F->inv_begin[l] + F->inv_count[l]; ++q)
+            if (info[nl + q] != 0) {
+                F->sing_kind = 2;
+                F->sing_index = F->inv_ids[q];
+                F->sing_info = info[nl + q];
+                return fail(DPLR_GPU_ESINGULAR, "capacitance %d is singular (zero pivot %d)", q - F->inv_begin[l],
+                            info[nl + q]);
+            }
+    return 0;
+}
+
+void factor_invalidate(Plan *p)
+{
+    if (p->fact) ((Fact *)p->fact)->valid = false;
+}
+
+Fact *factor_of(const Plan *p)
+{
+    Fact *F = (Fact *)p->fact;
+    return F && F->valid ? F : nullptr;
+}
+
+int factor_build(Plan *p, int flags, cudaStream_t st)
+{
+    Fact *F = (Fact *)p->fact;
+    if (!F || F->flags != flags || F->key_chunk != p->chunk_rows || F->key_nb != p->nb_cap) {
+        factor_free(p);
+        F = new Fact();
+        p->fact = F;
+        int rc0 = factor_layout(p, F, flags);
+        if (rc0) {
+            factor_free(p);
+            return rc0;
+        }
+    }
+    F->valid = false;
+    F->sing_kind = 0;
+    F->sing_index = -1;
+    F->sing_info = 0;
+    int rc;
+    const int nlev = (int)F->lv.size();
+    int lmax = 0;
+    for (const LeafDesc &Lf : p->leaves) lmax = std::max(lmax, Lf.b);
+
+    // Leaf inverses.
+    if (!p->leaves.empty()) {
+        copy_leaves_kernel<<<(unsigned)p->leaves.size(), 256, 0, st>>>(p->d_leaves, p->pool, F->d_leafoff,
+                                                                      F->leafinv);
+        note_launch();
+        DG_CUDA(cudaGetLastError());
+    }
+    if ((rc = batched_inverse(F->leafinv, F->d_leafoff, F->d_leafsize, (int)p->leaves.size(), lmax,
+                              F->d_info, F->leafdoubles, st)))
         return rc;
 
     // Levels bottom-up: Z_l (and Zt_l) through the already factored
@@ -539,7 +762,6 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
                 return rc;
         }
         // S V^T Z_l for the level's blocks, then K per node.
-        if ((rc = ensure_work(F, p, L.width))) return rc;
         double *T = F->work;
         double *partials = F->work + (size_t)2 * p->total_rank * L.width;
         if ((rc = run_panel(L.n, p->pool, F->zpool + F->zoff[l], p->m, L.width, partials, st))) return rc;
@@ -549,36 +771,23 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
                                                                          F->kpool);
             note_launch();
             DG_CUDA(cudaGetLastError());
-            // invert only this level's capacitance matrices
-            std::vector<long long> offs;
-            std::vector<int> sizes, ids;
-            for (int nd : L.nodes) {
-                const HDesc &H = p->nodes[nd];
-                int r = p->lr[H.ne].rank + p->lr[H.sw].rank;
-                if (r == 0) continue;
-                offs.push_back(F->koff[nd]);
-                sizes.push_back(r);
-                ids.push_back(nd);
-            }
-            long long *d_o = nullptr;
-            int *d_s = nullptr;
-            long long dummy = 0;
-            if ((rc = to_device(offs, &d_o, &dummy)) || (rc = to_device(sizes, &d_s, &dummy))) return rc;
-            rc = batched_inverse(F->kpool, d_o, d_s, (int)offs.size(), F->d_info, F->kdoubles, st,
-                                 "capacitance", F, 2, &ids);
-            cudaFree(d_o);
-            cudaFree(d_s);
-            if (rc) return rc;
+            // invert this level's capacitance matrices (info slots after the leaves')
+            const int b0 = F->inv_begin[l];
+            if ((rc = batched_inverse(F->kpool, F->d_inv_off + b0, F->d_inv_size + b0, F->inv_count[l],
+                                      F->inv_max[l], F->d_info + p->leaves.size() + b0, F->kdoubles, st)))
+                return rc;
         }
     }
     DG_CUDA(cudaStreamSynchronize(st));
+    if ((rc = factor_check(p, F))) return rc;
+    F->valid = true;
     return 0;
 }
 
 int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
                  cudaStream_t st)
 {
-    Fact *F = (Fact *)p->fact;
+    Fact *F = factor_of(p);
     if (!F) return fail(DPLR_GPU_ESTATE, "solve: plan is not factored");
     if (nrhs <= 0 || p->m == 0) return 0;
     return sweep(p, F, trans, 0, B, ldb, X, ldx, nrhs, st);

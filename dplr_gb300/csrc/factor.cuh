@@ -14,9 +14,23 @@ struct LevelOps {
     std::vector<int> nodes;    // HDesc indices at this level
 };
 
+struct ScatterItem;
+
 struct Fact {
     int flags = 0;
     bool transposed = false;
+    // the numbers are current (cleared when the plan's values change; the
+    // layout below is kept and reused by the next factorisation)
+    bool valid = false;
+    int key_chunk = 0, key_nb = 0;    // schedule parameters the layout was built with
+    // per level: the level right-hand side's scatter items (U: [0], V: [1])
+    // and the capacitance inverses (offsets, orders, node ids), all levels
+    // in one device array each
+    ScatterItem *d_scat = nullptr;
+    std::vector<int> scat_begin[2], scat_count[2], scat_max[2];
+    long long *d_inv_off = nullptr;
+    int *d_inv_size = nullptr;
+    std::vector<int> inv_begin, inv_count, inv_max, inv_ids;
     std::vector<LevelOps> lv;
     std::vector<long long> zoff;      // per level, offset in zpool / ztpool
     long long zdoubles = 0;
@@ -48,6 +62,11 @@ struct Fact {
 
 int factor_build(Plan *p, int flags, cudaStream_t st);
 void factor_free(Plan *p);
+// The plan's values changed: the factorisation's numbers are stale; its
+// layout is kept for the next factor_build.
+void factor_invalidate(Plan *p);
+// The plan's factorisation when its numbers are current, else nullptr.
+Fact *factor_of(const Plan *p);
 int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
                  cudaStream_t st);
 long long factor_bytes(const Plan *p);

@@ -177,12 +177,13 @@ int grad_factors(Plan *p, int nrhs, const double *X, int ldx, const double *DY, 
     return 0;
 }
 
-// The factor values changed on the device: drop everything derived from them.
+// The factor values changed on the device: drop everything derived from
+// them (the factorisation keeps its layout for the next factor_build).
 void plan_values_changed(Plan *p)
 {
     mixed_free(p);
     sliced_free(p);
-    factor_free(p);
+    factor_invalidate(p);
 }
 
 }  // namespace dg

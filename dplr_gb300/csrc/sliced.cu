@@ -1217,7 +1217,7 @@ out:
 int mixed_build(Plan *p, int ns, cudaStream_t st, bool fp64_caps)
 {
     mixed_free(p);
-    Fact *F = (Fact *)p->fact;
+    Fact *F = factor_of(p);
     if (!F) return fail(DPLR_GPU_ESTATE, "mixed solve: plan is not factored");
     if (ns < kMSMin || ns > kMSMax)
         return fail(DPLR_GPU_EINVAL, "mixed solve: %d slices (supported: %d to %d)", ns, kMSMin, kMSMax);
@@ -1500,7 +1500,7 @@ static int mixed_solve_t(Plan *p, MixedSliced *M, Fact *F, int nrhs, const doubl
 int mixed_solve(Plan *p, int nrhs, const double *B, int ldb, double *X, int ldx, cudaStream_t st)
 {
     MixedSliced *M = (MixedSliced *)p->mixed;
-    Fact *F = (Fact *)p->fact;
+    Fact *F = factor_of(p);
     if (!M || !F) return fail(DPLR_GPU_ESTATE, "mixed solve: not prepared");
     if (nrhs <= 0 || p->m == 0) return 0;
     if (M->leaf.tile_m == tc::M) {

@@ -20,6 +20,8 @@ int factor_build(Plan *p, int flags, cudaStream_t st);
 int factor_solve(Plan *p, int trans, int nrhs, const double *B, int ldb, double *X, int ldx,
                  cudaStream_t st);
 long long factor_bytes(const Plan *p);
+struct Fact;
+Fact *factor_of(const Plan *p);
 
 // Column 2-norms of an m x n matrix: one CTA of kNormThreads per column,
 // four independent sums per thread so that four loads are in flight (one
@@ -151,6 +153,135 @@ static int segnorms_device(Plan *p, const double *A, int n, int lda, double *out
     return 0;
 }
 
+// X's copy to a host array on a side stream, while the refinement goes
+// on: the copy of each iterate starts as soon as it exists and overlaps the
+// residual that checks it; the next update of X waits for it.  The stream
+// is drained (and destroyed) on every way out, so no copy lands after the
+// call has returned.
+struct HostCopy {
+    double *hX = nullptr;
+    int ldhx = 0;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    bool pending = false;
+    ~HostCopy()
+    {
+        if (cs) cudaStreamSynchronize(cs);
+        if (ready) cudaEventDestroy(ready);
+        if (done) cudaEventDestroy(done);
+        if (cs) cudaStreamDestroy(cs);
+    }
+    int init(double *h, int ld)
+    {
+        hX = h;
+        ldhx = ld;
+        if (!hX) return 0;
+        if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess)
+            return fail(DPLR_GPU_ECUDA, "refined solve: cannot create the copy stream");
+        return 0;
+    }
+    // X (m x n, ld ldx on the device) is final for now: copy it out
+    int start(const double *X, int ldx, int m, int n, cudaStream_t st)
+    {
+        if (!hX) return 0;
+        DG_CUDA(cudaEventRecord(ready, st));
+        DG_CUDA(cudaStreamWaitEvent(cs, ready, 0));
+        DG_CUDA(cudaMemcpy2DAsync(hX, sizeof(double) * ldhx, X, sizeof(double) * ldx, sizeof(double) * m, n,
+                                  cudaMemcpyDeviceToHost, cs));
+        DG_CUDA(cudaEventRecord(done, cs));
+        pending = true;
+        return 0;
+    }
+    // X is about to change on st: wait for its copy
+    int before_write(cudaStream_t st)
+    {
+        if (!hX || !pending) return 0;
+        DG_CUDA(cudaStreamWaitEvent(st, done, 0));
+        return 0;
+    }
+    int finish()
+    {
+        if (!hX) return 0;
+        DG_CUDA(cudaStreamSynchronize(cs));
+        return 0;
+    }
+};
+
+// The refinement loop of dplr_gpu_solve_refined; with hX, every iterate of
+// X is also copied to the host array hX (ld ldhx), and the last one is there
+// when it returns.
+static int refine(Plan *p, int n, const double *B, int ldb, double *X, int ldx, double tol, int maxiter, int flags,
+                  double *rel_resid, int *iters, cudaStream_t st, double *hX, int ldhx)
+{
+    if (n == 0 || p->m == 0) {
+        if (rel_resid) *rel_resid = 0.0;
+        if (iters) *iters = 0;
+        return 0;
+    }
+    const int m = p->m;
+    // Scratch: residual R, correction D (m x n each), the norms of B and R
+    // per column and tree: a batch converges when every tree's every column
+    // does, not on the norms of the stacked columns.
+    const size_t nn = (size_t)n * std::max(p->ntrees, 1);
+    size_t need = (size_t)2 * m * n + 2 * nn;
+    int rc = ensure_buffer(&p->ybuf, &p->ybuf_doubles, need);
+    if (rc) return rc;
+    double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
+    double *bn = D + (size_t)m * n, *rn = bn + nn;
+    std::vector<double> hb(nn), hr(nn);
+    const bool mixed = (flags & DPLR_GPU_SOLVE_MIXED) != 0;
+    if (mixed && !p->mixed) return fail(DPLR_GPU_ESTATE, "solve: mixed solve not prepared");
+    if ((flags & DPLR_GPU_RESIDUAL_SLICED) && !p->sliced)
+        return fail(DPLR_GPU_ESTATE, "solve: sliced residual not prepared");
+    HostCopy hc;
+    if ((rc = hc.init(hX, ldhx))) return rc;
+    auto inner = [&](const double *rhs, int ld, double *out, int ldo) -> int {
+        return mixed ? mixed_solve(p, n, rhs, ld, out, ldo, st) : factor_solve(p, 0, n, rhs, ld, out, ldo, st);
+    };
+    if ((rc = segnorms_device(p, B, n, ldb, bn, st))) return rc;
+    DG_CUDA(cudaMemcpyAsync(hb.data(), bn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if ((rc = inner(B, ldb, X, ldx))) return rc;
+    if ((rc = hc.start(X, ldx, m, n, st))) return rc;
+    double worst = INFINITY;
+    int it = 0;
+    for (;;) {
+        // R = B - A X with the original matrix (FP64 apply, or exact-slice products)
+        if (flags & DPLR_GPU_RESIDUAL_SLICED) {
+            if ((rc = sliced_residual(p, n, X, ldx, B, ldb, R, m, st))) return rc;
+        } else {
+            if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
+            if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
+        }
+        {
+            ProfScope ps("refine_norms", st, 0.0, 8.0 * m * n);
+            if ((rc = segnorms_device(p, R, n, m, rn, st))) return rc;
+        }
+        DG_CUDA(cudaMemcpyAsync(hr.data(), rn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        if ((rc = sliced_error(p))) return rc;
+        worst = 0.0;
+        for (size_t j = 0; j < nn; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
+        if (worst <= tol || it >= maxiter) break;
+        if ((rc = inner(R, m, D, m))) return rc;
+        {
+            ProfScope ps("refine_update", st, 0.0, 24.0 * m * n);
+            if ((rc = hc.before_write(st))) return rc;
+            if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
+        }
+        if ((rc = hc.start(X, ldx, m, n, st))) return rc;
+        ++it;
+    }
+    if ((rc = hc.finish())) return rc;
+    if (rel_resid) *rel_resid = worst;
+    if (iters) *iters = it;
+    if (!(worst <= tol))
+        return fail(DPLR_GPU_ENOTCONV, "refinement stopped at relative residual %.3e after %d steps",
+                    worst, it);
+    return 0;
+}
+
 }  // namespace dg
 
 using namespace dg;
@@ -224,69 +355,10 @@ int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, int ldb, 
     dg::NvtxRange nvtx_("dplr_gpu_solve_refined");
     Plan *p = (Plan *)plan;
     if (!p) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: null plan");
-    if (!p->fact) return fail(DPLR_GPU_ESTATE, "dplr_gpu_solve_refined: plan is not factored");
+    if (!factor_of(p)) return fail(DPLR_GPU_ESTATE, "dplr_gpu_solve_refined: plan is not factored");
     if (n < 0 || ldb < std::max(p->m, 1) || ldx < std::max(p->m, 1) || maxiter < 0)
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined: invalid arguments");
-    if (n == 0 || p->m == 0) {
-        if (rel_resid) *rel_resid = 0.0;
-        if (iters) *iters = 0;
-        return 0;
-    }
-    cudaStream_t st = (cudaStream_t)stream;
-    const int m = p->m;
-    // Scratch: residual R, correction D (m x n each), the norms of B and R
-    // per column and tree: a batch converges when every tree's every column
-    // does, not on the norms of the stacked columns.
-    const size_t nn = (size_t)n * std::max(p->ntrees, 1);
-    size_t need = (size_t)2 * m * n + 2 * nn;
-    int rc = ensure_buffer(&p->ybuf, &p->ybuf_doubles, need);
-    if (rc) return rc;
-    double *R = p->ybuf, *D = p->ybuf + (size_t)m * n;
-    double *bn = D + (size_t)m * n, *rn = bn + nn;
-    std::vector<double> hb(nn), hr(nn);
-    const bool mixed = (flags & DPLR_GPU_SOLVE_MIXED) != 0;
-    if (mixed && !p->mixed) return fail(DPLR_GPU_ESTATE, "solve: mixed solve not prepared");
-    if ((flags & DPLR_GPU_RESIDUAL_SLICED) && !p->sliced)
-        return fail(DPLR_GPU_ESTATE, "solve: sliced residual not prepared");
-    auto inner = [&](const double *rhs, int ld, double *out, int ldo) -> int {
-        return mixed ? mixed_solve(p, n, rhs, ld, out, ldo, st) : factor_solve(p, 0, n, rhs, ld, out, ldo, st);
-    };
-    if ((rc = segnorms_device(p, B, n, ldb, bn, st))) return rc;
-    DG_CUDA(cudaMemcpyAsync(hb.data(), bn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if ((rc = inner(B, ldb, X, ldx))) return rc;
-    double worst = INFINITY;
-    int it = 0;
-    for (;;) {
-        // R = B - A X with the original matrix (FP64 apply, or exact-slice products)
-        if (flags & DPLR_GPU_RESIDUAL_SLICED) {
-            if ((rc = sliced_residual(p, n, X, ldx, B, ldb, R, m, st))) return rc;
-        } else {
-            if ((rc = axpby_device(m, n, 1.0, B, ldb, 0.0, R, m, st))) return rc;
-            if ((rc = apply_device(p, 0, n, -1.0, X, ldx, 1.0, R, m, st, false))) return rc;
-        }
-        {
-            ProfScope ps("refine_norms", st, 0.0, 8.0 * m * n);
-            if ((rc = segnorms_device(p, R, n, m, rn, st))) return rc;
-        }
-        DG_CUDA(cudaMemcpyAsync(hr.data(), rn, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
-        DG_CUDA(cudaStreamSynchronize(st));
-        if ((rc = sliced_error(p))) return rc;
-        worst = 0.0;
-        for (size_t j = 0; j < nn; ++j) worst = std::max(worst, hb[j] > 0 ? hr[j] / hb[j] : hr[j]);
-        if (worst <= tol || it >= maxiter) break;
-        if ((rc = inner(R, m, D, m))) return rc;
-        {
-            ProfScope ps("refine_update", st, 0.0, 24.0 * m * n);
-            if ((rc = axpby_device(m, n, 1.0, D, m, 1.0, X, ldx, st))) return rc;
-        }
-        ++it;
-    }
-    if (rel_resid) *rel_resid = worst;
-    if (iters) *iters = it;
-    if (!(worst <= tol))
-        return fail(DPLR_GPU_ENOTCONV, "refinement stopped at relative residual %.3e after %d steps",
-                    worst, it);
-    return 0;
+    return refine(p, n, B, ldb, X, ldx, tol, maxiter, flags, rel_resid, iters, (cudaStream_t)stream, nullptr, 0);
 }
 
 int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb, double *X,
@@ -300,6 +372,8 @@ int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int 
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: invalid arguments");
     if (n == 0 || p->m == 0) return dplr_gpu_solve_refined(plan, n, nullptr, 1, nullptr, 1, tol,
                                                           maxiter, flags, rel_resid, iters, stream);
+    if (!factor_of(p)) return fail(DPLR_GPU_ESTATE, "dplr_gpu_solve_refined_host: plan is not factored");
+    if (maxiter < 0) return fail(DPLR_GPU_EINVAL, "dplr_gpu_solve_refined_host: invalid arguments");
     cudaStream_t st = (cudaStream_t)stream;
     const size_t cnt = (size_t)p->m * n;
     int rc = ensure_buffer(&p->xbuf, &p->xbuf_doubles, 2 * cnt);
@@ -307,16 +381,11 @@ int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int 
     double *dB = p->xbuf, *dX = p->xbuf + cnt;
     // one copy each way: measured on the GB300, pinned copies run at the
     // link's 210 GB/s (host to device) and 193 GB/s (device to host) whether
-    // issued on one stream or split over four
+    // issued on one stream or split over four.  X goes back while the
+    // refinement checks it (see refine).
     DG_CUDA(cudaMemcpy2DAsync(dB, sizeof(double) * p->m, B, sizeof(double) * ldb,
                               sizeof(double) * p->m, n, cudaMemcpyHostToDevice, st));
-    rc = dplr_gpu_solve_refined(plan, n, dB, p->m, dX, p->m, tol, maxiter, flags, rel_resid, iters,
-                                stream);
-    if (rc && rc != DPLR_GPU_ENOTCONV) return rc;
-    DG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, dX, sizeof(double) * p->m,
-                              sizeof(double) * p->m, n, cudaMemcpyDeviceToHost, st));
-    DG_CUDA(cudaStreamSynchronize(st));
-    return rc;
+    return refine(p, n, dB, p->m, dX, p->m, tol, maxiter, flags, rel_resid, iters, st, X, ldx);
 }
 
 long long dplr_gpu_factor_device_bytes(dplr_gpu_plan plan)

@@ -169,7 +169,10 @@ DPLR_API int dplr_gpu_solve_refined(dplr_gpu_plan plan, int n, const double *B, 
 /* The same refined solve with B and X in host memory (column-major,
  * leading dimensions ldb, ldx >= m): B is copied to the device, solved and
  * X copied back inside the call (pinned host memory makes the copies
- * asynchronous DMA). */
+ * asynchronous DMA).  Each iterate of X starts back to the host while the
+ * refinement checks it, so the last copy overlaps the last residual; X
+ * holds the last iterate when the call returns (also on
+ * DPLR_GPU_ENOTCONV; after another error it may hold an earlier one). */
 DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double *B, int ldb,
                                          double *X, int ldx, double tol, int maxiter, int flags,
                                          double *rel_resid, int *iters, void *stream);

@@ -93,3 +93,31 @@ def test_singular_leaf_reported():
     with pytest.raises(_native.NativeError, match="singular"):
         p.factor()
     p.close()
+
+
+@pytest.mark.parametrize("maxiter", [0, 3])
+def test_refined_solve_with_host_buffers(maxiter):
+    """dplr_gpu_solve_refined_host (B and X in host memory, X copied back
+    while the refinement checks each iterate) returns the device path's X
+    bit for bit, with its residual and correction count, whether it stops
+    converged or at maxiter (DPLR_GPU_ENOTCONV, X the last iterate)."""
+    import ctypes
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+    t = CASES["exp4k"]()
+    m = t.size
+    p = GpuPlan(t)
+    p.factor()
+    b = np.random.default_rng(8).standard_normal((5, m))
+    tol = 1e-12 if maxiter else 1e-30
+    xd, res_d, its_d = p.solve_refined(torch.tensor(b, device="cuda"), tol=tol, maxiter=maxiter, precise=False,
+                                       strict=False)
+    bh = torch.tensor(b).pin_memory()
+    xh = torch.full((5, m), np.nan, dtype=torch.float64).pin_memory()
+    res, its = ctypes.c_double(), ctypes.c_int()
+    rc = _native.lib().dplr_gpu_solve_refined_host(p.handle, 5, bh.data_ptr(), m, xh.data_ptr(), m, tol, maxiter,
+                                                   0, ctypes.byref(res), ctypes.byref(its), None)
+    assert rc == (0 if maxiter else -5)
+    assert torch.equal(xh, xd.cpu())
+    assert res.value == res_d and its.value == its_d
+    p.close()
