@@ -317,7 +317,8 @@ def batched_workload(steps: int, warmup: int, count: int = 512) -> dict:
                                "autotune": grp["tune"]} for grp in groups],
                    "refined_solve_max_rel_resid": worst,
                    "refined_solve_exact_residual": {
-                       "ms": exact_ms, "max_rel_resid": exact_worst, "kernels": exact_kernels,
+                       "ms": exact_ms, "rhs_per_s": total_rhs / (exact_ms / 1e3) if exact_ms > 0 else None,
+                       "max_rel_resid": exact_worst, "kernels": exact_kernels,
                        "note": "the same refined-solve graphs with exact-slice residuals in the corrections "
                                "(tcgen05 kernels; the 64-row leaves and blocks are stored as half-empty "
                                "128-row tiles)"},
