@@ -30,6 +30,7 @@ int run_op(Plan *p, char op, int trans, int n, const double *X, int ldx, double 
 {
     if (op == 'A' || op == 'a') return apply_device(p, trans, n, 1.0, X, ldx, 0.0, Y, ldy, st, false);
     if (op == 'R' || op == 'r') return refine_fixed(p, n, X, ldx, Y, ldy, 2, st);
+    if (op == 'C' || op == 'c') return refine_fixed(p, n, X, ldx, Y, ldy, 1, st);
     return factor_solve(p, trans, n, X, ldx, Y, ldy, st);
 }
 
@@ -81,11 +82,11 @@ int dplr_gpu_graph_create(dplr_gpu_plan plan, char op, char trans, int n, const 
     const int mm = std::max(p->m, 1);
     if (n <= 0 || ldx < mm || ldy < mm || !X || !Y || X == Y)
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: invalid n, leading dimension or pointers");
-    if (!(op == 'A' || op == 'a' || op == 'S' || op == 's' || op == 'R' || op == 'r'))
-        return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: op must be 'A' (apply), 'S' (solve) or 'R' "
-                                     "(solve with two refinement steps)");
+    if (!(op == 'A' || op == 'a' || op == 'S' || op == 's' || op == 'R' || op == 'r' || op == 'C' || op == 'c'))
+        return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: op must be 'A' (apply), 'S' (solve), 'C' (solve "
+                                     "with one refinement step) or 'R' (two refinement steps)");
     const int tr = !(trans == 'N' || trans == 'n');
-    if ((op == 'R' || op == 'r') && tr)
+    if ((op == 'R' || op == 'r' || op == 'C' || op == 'c') && tr)
         return fail(DPLR_GPU_EINVAL, "dplr_gpu_graph_create: the refined solve is op N only");
     GraphH *g = new GraphH();
     auto bail = [&](int rc) {

@@ -243,8 +243,9 @@ DPLR_API int dplr_gpu_batch_offsets(dplr_gpu_plan plan, int *count, int *row0);
  * Y = op(A)^-1 X, needs dplr_gpu_factor) or one solve refined by two
  * correction steps (op 'R', trans 'N': Y = A^-1 X, twice R = X - A Y with the
  * exact-slice products if dplr_gpu_prepare_sliced was called, else the FP64
- * apply, Y += A^-1 R; no host synchronisation inside, so the whole refined
- * solve is one replay; dplr_gpu_residual checks the result) with fixed
+ * apply, Y += A^-1 R; op 'C': the same with one correction step; no host
+ * synchronisation inside, so the whole refined solve is one replay;
+ * dplr_gpu_residual checks the result) with fixed
  * device arrays: built
  * once (one ordinary run sizes the scratch, a second run is captured on an
  * internal stream), then replayed by dplr_gpu_graph_launch on any stream

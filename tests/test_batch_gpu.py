@@ -151,3 +151,26 @@ def test_refined_solve_converges_per_matrix():
         rr, bb = r[:, o:o + t.size], b[:, o:o + t.size]
         assert float((rr.norm(dim=1) / bb.norm(dim=1)).max()) <= 1e-11
     batch.close()
+
+
+@pytest.mark.parametrize("op,corrections", [("C", 1), ("R", 2)])
+def test_refined_graph_replays_the_refined_solve(op, corrections):
+    """Graph ops 'C' and 'R' replay the solve with one or two correction
+    steps (FP64 residuals, no host synchronisation inside): bit for bit the
+    iterates of dplr_gpu_solve_refined stopped after as many corrections."""
+    from dplr_gb300.plan import GpuGraph, GpuPlan
+    trees = _trees(6, 5)
+    batch = GpuPlan.batch(trees)
+    batch.factor()
+    X = _rhs(batch.m, 4, 9)
+    want, _, its = batch.solve_refined(X, tol=0.0, maxiter=corrections, precise=False, strict=False)
+    assert its == corrections
+    Y = torch.zeros_like(X)
+    g = GpuGraph(batch, op, X, Y)
+    for _ in range(2):
+        Y.zero_()
+        g.launch()
+        torch.cuda.synchronize()
+        assert torch.equal(Y, want)
+    g.close()
+    batch.close()
