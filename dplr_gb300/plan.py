@@ -316,8 +316,9 @@ class GpuPlan:
 
 
 class GpuGraph:
-    """A captured CUDA graph of one apply ('A') or solve ('S') of a plan with
-    fixed tensors x (input) and y (output); launch() replays it."""
+    """A captured CUDA graph of one apply ('A'), solve ('S'), or solve
+    refined by one ('C') or two ('R') correction steps of a plan, with fixed
+    tensors x (input) and y (output); launch() replays it."""
 
     def __init__(self, plan: GpuPlan, op: str, x: torch.Tensor, y: torch.Tensor, trans: str = "N",
                  stream=None):
