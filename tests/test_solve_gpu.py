@@ -121,3 +121,36 @@ def test_refined_solve_with_host_buffers(maxiter):
     assert torch.equal(xh, xd.cpu())
     assert res.value == res_d and its.value == its_d
     p.close()
+
+
+def test_refactorisation_after_new_values_reuses_the_layout():
+    """New factor values (dplr_gpu_pool_write) keep the factorisation's
+    layout: the next factor() recomputes the numbers only.  The solve after
+    a refactorisation of the same values is bit-identical; a singular leaf
+    written in between is reported (and the plan refuses to solve), and
+    restoring the values makes the plan factor and solve again."""
+    from dplr_gb300 import _native
+    from dplr_gb300.plan import GpuPlan
+    t = gen.random_tree(1024, 64, [12, 8, 4, 2], seed=11)
+    p = GpuPlan(t)
+    p.factor()
+    b = torch.randn(3, t.size, dtype=torch.float64, device="cuda")
+    x0 = p.solve(b).clone()
+    xt0 = p.solve(b, trans="T").clone()
+    pool = p.read_pool()
+    p.write_pool(pool)
+    p.factor()
+    assert torch.equal(p.solve(b), x0)
+    assert torch.equal(p.solve(b, trans="T"), xt0)
+    leaf = next(blk for blk in p.pool_blocks() if blk["kind"] == "leaf")
+    bad = pool.clone()
+    bad[leaf["d"]:leaf["d"] + leaf["b"] * leaf["b"]] = 0.0
+    p.write_pool(bad)
+    with pytest.raises(_native.NativeError, match="singular"):
+        p.factor()
+    with pytest.raises(_native.NativeError, match="not factored"):
+        p.solve(b)
+    p.write_pool(pool)
+    p.factor()
+    assert torch.equal(p.solve(b), x0)
+    p.close()
