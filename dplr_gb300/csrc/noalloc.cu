@@ -2,8 +2,6 @@
 //
 // Some callers of this library cannot allocate device memory at the moment
 // they need an apply:
-//   * code being recorded into a CUDA graph by stream capture, where
-//     cudaMalloc is not a stream operation and must not be called;
 //   * latency-critical serving paths that must never pay for cudaMalloc or
 //     the device-wide synchronisation cudaFree can imply;
 //   * host frameworks that hand the library a fixed device-memory budget up
@@ -26,8 +24,7 @@
 //   * the array keeps whatever the previous call left; every element a call
 //     reads is written earlier in the same call, so nothing is cleared;
 //   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current).  Make that first call
-//     before any stream capture that is to contain later calls.
+//     (cudaGetSymbolAddress, with that device current) and keeps it.
 #include "internal.cuh"
 
 #include <mutex>

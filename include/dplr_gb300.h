@@ -179,15 +179,15 @@ DPLR_API int dplr_gpu_solve_refined_host(dplr_gpu_plan plan, int n, const double
 
 /* Y := alpha*op(A)*X + beta*Y like dplr_gpu_apply, but without allocating
  * any device memory.  No counterpart in DPLR (whose routines malloc per
- * block visit).  For callers that cannot allocate when they apply: code
- * recorded by CUDA stream capture, latency-critical paths that must avoid
- * cudaMalloc/cudaFree and their implicit synchronisation, and hosts that
- * fix the library's device memory in advance.  Scratch is a static 64 MiB
+ * block visit).  For callers that cannot allocate when they apply:
+ * latency-critical paths that must avoid cudaMalloc/cudaFree and their
+ * implicit synchronisation, and hosts that fix the library's device memory
+ * in advance.  Scratch is a static 64 MiB
  * device array shared by all calls on a device: calls that may overlap on
  * the GPU race and must be ordered by the caller; a call needing more
  * scratch than that, (sum of ranks + partial panels) * n doubles, fails
  * with DPLR_GPU_EINVAL.  The first call on a device resolves the array's
- * address and should come before any stream capture.  That address is kept
+ * address (cudaGetSymbolAddress).  That address is kept
  * for the life of the process: it assumes one CUDA context per device (the
  * primary context, not reset with cudaDeviceReset in between).  The array's
  * contents are never read before a call writes them, and its 64 MiB are

@@ -1,7 +1,7 @@
 """dplr_gpu_apply_noalloc: the apply for callers that cannot allocate.
 
-Callers recording CUDA graphs by stream capture, latency-critical paths that
-must not call cudaMalloc/cudaFree, and hosts with a fixed device-memory
+Latency-critical paths that must not call cudaMalloc/cudaFree, and hosts
+with a fixed device-memory
 budget use this entry point; its scratch is a static device array inside
 the library.  It must give the same result as dplr_gpu_apply (1e-12
 relative, the tolerance of the apply tests) on two calls in a row, and
