@@ -475,32 +475,18 @@ __global__ void __launch_bounds__(kSThreads) sp_panel_kernel(
 // the ranks), and the chunk sums run four loads deep (integer sums, so the
 // order does not change the result).
 template <int DMAX>
-__global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items, int nitems, long long total,
+__global__ void sp_reduce_kernel(const SReduceItem *__restrict__ items, const int *__restrict__ rank_item,
+                                 long long total,
                                  const __int128 *__restrict__ partials, const int *__restrict__ aexp,
                                  const int *__restrict__ xexp, const double *__restrict__ sigbase,
                                  int nrhs, double *__restrict__ T, long long lo_off)
 {
     const long long E = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    // the item holding the CTA's first element (one binary search per CTA),
-    // then each thread steps forward from it: a CTA's 256 consecutive
-    // elements span one item or a few small ones.  The element within the
-    // item costs one 32-bit division (rank * nrhs of one item stays below
-    // 2^31).
-    __shared__ int first;
-    if (threadIdx.x == 0) {
-        const long long E0 = (long long)blockIdx.x * blockDim.x;
-        int lo = 0, hi = nitems - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((long long)items[mid].rsum * nrhs <= E0) lo = mid; else hi = mid - 1;
-        }
-        first = lo;
-    }
-    __syncthreads();
     if (E >= total) return;
-    int lo = first;
-    while (lo + 1 < nitems && (long long)items[lo + 1].rsum * nrhs <= E) ++lo;
-    const SReduceItem R = items[lo];
+    // the item from the rank-position table (element E sits at position
+    // E / nrhs); the element within the item costs one 32-bit division
+    // (rank * nrhs of one item stays below 2^31)
+    const SReduceItem R = items[rank_item[E / nrhs]];
     const long long cnt = (long long)R.rank * nrhs;
     const int e = (int)(E - (long long)R.rsum * nrhs);
     const int j = e / R.rank, k = e - j * R.rank;
@@ -536,7 +522,7 @@ static void launch_reduce(const SSchedule &S, const __int128 *partials, const in
     const long long total = (long long)S.rtotal * nrhs;
     if (S.reduces.empty() || total == 0) return;
     sp_reduce_kernel<DMAX><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
-        S.d_reduces, (int)S.reduces.size(), total, partials, aexp, xexp, sigbase, nrhs, T, lo_off);
+        S.d_reduces, S.d_rank_item, total, partials, aexp, xexp, sigbase, nrhs, T, lo_off);
     note_launch();
 }
 
@@ -806,6 +792,8 @@ static void free_sschedule(SSchedule &A)
     A.d_rmax = nullptr;
     cudaFree(A.d_items);
     cudaFree(A.d_reduces);
+    cudaFree(A.d_rank_item);
+    A.d_rank_item = nullptr;
     cudaFree(A.d_tile_row0);
     cudaFree(A.d_tile_begin);
     cudaFree(A.d_terms);
@@ -831,14 +819,27 @@ void sliced_free(Plan *p)
 
 static size_t panel_smem(int nsa, int nsb) { return (size_t)(nsa + nsb) * ST * SLD * sizeof(bf16); }
 
+// The reduce's element space: item i owns the rank positions [rsum_i,
+// rsum_i + rank_i); the table maps each position to its item, so that a
+// reduce thread finds its item with one load (element E is at position
+// E / nrhs).
+static int upload_rank_items(SSchedule &A, long long *bytes)
+{
+    A.rtotal = 0;
+    std::vector<int> owner;
+    for (size_t i = 0; i < A.reduces.size(); ++i) {
+        SReduceItem &r = A.reduces[i];
+        r.rsum = A.rtotal;
+        A.rtotal += r.rank;
+        owner.insert(owner.end(), r.rank, (int)i);
+    }
+    return dev_vec(owner, &A.d_rank_item, bytes);
+}
+
 static int upload_sschedule(SSchedule &A, long long *bytes)
 {
     int rc;
-    A.rtotal = 0;
-    for (SReduceItem &r : A.reduces) {
-        r.rsum = A.rtotal;
-        A.rtotal += r.rank;
-    }
+    if ((rc = upload_rank_items(A, bytes))) return rc;
     if ((rc = dev_vec(A.items, &A.d_items, bytes)) || (rc = dev_vec(A.reduces, &A.d_reduces, bytes)) ||
         (rc = dev_vec(A.tile_row0, &A.d_tile_row0, bytes)) ||
         (rc = dev_vec(A.tile_begin, &A.d_tile_begin, bytes)) || (rc = dev_vec(A.terms, &A.d_terms, bytes)))
@@ -1824,11 +1825,7 @@ __global__ void tile_cmax_kernel(const XTerm *__restrict__ terms, const int *__r
 int upload_tb(SSchedule &S, long long *bytes)
 {
     int rc;
-    S.rtotal = 0;
-    for (SReduceItem &r : S.reduces) {
-        r.rsum = S.rtotal;
-        S.rtotal += r.rank;
-    }
+    if ((rc = upload_rank_items(S, bytes))) return rc;
     if ((rc = dev_vec(S.pitems, &S.d_pitems, bytes)) || (rc = dev_vec(S.reduces, &S.d_reduces, bytes)) ||
         (rc = dev_vec(S.tile_row0, &S.d_tile_row0, bytes)) || (rc = dev_vec(S.tile_begin, &S.d_tile_begin, bytes)) ||
         (rc = dev_vec(S.xterms, &S.d_xterms, bytes)))

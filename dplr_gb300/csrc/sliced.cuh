@@ -94,6 +94,7 @@ struct SSchedule {
     long long tpad_per_rhs = 0;     // T-slice entries / nrhs
     int max_rank = 0;
     int rtotal = 0;                 // sum of the reduce items' ranks
+    int *d_rank_item = nullptr;     // per rank position (rsum + k) its reduce item
     std::vector<int> tile_row0, tile_begin;
     std::vector<STerm> terms;
     SPanelItem *d_items = nullptr;
