@@ -325,9 +325,10 @@ static int zero_device(double *p, long long n, cudaStream_t st)
 // kSmemInvMax the matrices are inverted in shared memory, else in place in
 // global memory with a scratch of `span` doubles (freed in stream order).
 static int batched_inverse(double *base, long long *d_off, int *d_size, int count, int nmax, int *d_info,
-                           long long span, cudaStream_t st)
+                           long long span, cudaStream_t st, double flops)
 {
     if (count == 0) return 0;
+    ProfScope ps("inverse", st, flops, 0.0);       // LU + inverse: 2 n^3 per matrix
     if (nmax <= kSmemInvMax) {
         const int smem = (nmax * nmax + nmax) * (int)sizeof(double);
         DG_CUDA(cudaFuncSetAttribute(lu_inverse_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -744,8 +745,10 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
         note_launch();
         DG_CUDA(cudaGetLastError());
     }
+    double lfl = 0.0;
+    for (const LeafDesc &Lf : p->leaves) lfl += 2.0 * Lf.b * Lf.b * (double)Lf.b;
     if ((rc = batched_inverse(F->leafinv, F->d_leafoff, F->d_leafsize, (int)p->leaves.size(), lmax,
-                              F->d_info, F->leafdoubles, st)))
+                              F->d_info, F->leafdoubles, st, lfl)))
         return rc;
 
     // Levels bottom-up: Z_l (and Zt_l) through the already factored
@@ -773,8 +776,14 @@ int factor_build(Plan *p, int flags, cudaStream_t st)
             DG_CUDA(cudaGetLastError());
             // invert this level's capacitance matrices (info slots after the leaves')
             const int b0 = F->inv_begin[l];
+            double kfl = 0.0;
+            for (int q = b0; q < b0 + F->inv_count[l]; ++q) {
+                const HDesc &H = p->nodes[F->inv_ids[q]];
+                const double r = p->lr[H.ne].rank + p->lr[H.sw].rank;
+                kfl += 2.0 * r * r * r;
+            }
             if ((rc = batched_inverse(F->kpool, F->d_inv_off + b0, F->d_inv_size + b0, F->inv_count[l],
-                                      F->inv_max[l], F->d_info + p->leaves.size() + b0, F->kdoubles, st)))
+                                      F->inv_max[l], F->d_info + p->leaves.size() + b0, F->kdoubles, st, kfl)))
                 return rc;
         }
     }

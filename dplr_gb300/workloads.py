@@ -375,6 +375,14 @@ def adjoint_workload(steps: int, warmup: int, n: int = 65536) -> dict:
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    launches = _native.launch_count() - l0
+    # algorithmic FP64 work of one step, from the profiled launches
+    _native.profile_start()
+    step()
+    prof = _native.profile_stop()
+    flops = sum(v[1] for v in prof.values())
+    fp64 = fp64_gemm_peak()
+    tflops = flops / (ms / 1e3) / 1e12
     # spot check against central differences (h = 1e-6) on two factor entries
     blocks = plan.pool_blocks()
     idx = [blocks[0]["u"] + 7, blocks[len(blocks) // 2]["d"] if "d" in blocks[len(blocks) // 2]
@@ -391,10 +399,17 @@ def adjoint_workload(steps: int, warmup: int, n: int = 65536) -> dict:
     return {
         "metric": "adjoint steps/s: loss=||A^-1 b - t||^2 and gradients (b, U, V, sig, leaves) @N=65536",
         "value": 1000.0 / ms, "unit": "steps/s", "ms_per_step": ms, "higher_is_better": True,
-        "dtype": "f64", "gpu_launches": _native.launch_count() - l0,
+        "dtype": "f64", "gpu_launches": launches,
+        "roofline": {"kernel": "whole step (factorisation: leaf and capacitance inverses, truncated sweeps; "
+                               "solve, transposed solve)", "bound": "fp64", "achieved": tflops,
+                     "peak": fp64["tflops"], "unit": "TFLOP/s", "frac": tflops / fp64["tflops"], "traffic": None,
+                     "peak_source": "of " + fp64["source"],
+                     "algorithmic": f"{flops:.4g} flop per step (the profiled launches' algorithmic counts; "
+                                    f"inverses at 2 n^3)"},
         "config": {"workload": "1D exponential kernel, N=65536, leaf 128, rank 16; factorisation, solve, "
                                "transposed solve and factor gradient per step",
-                   "pool_doubles": plan.pool_size(), "loss": float(loss), "fd_check": fd},
+                   "pool_doubles": plan.pool_size(), "loss": float(loss), "fd_check": fd,
+                   "kernels_ms": {k: v[0] for k, v in prof.items()}},
     }
 
 
@@ -597,6 +612,14 @@ def ppmm_workload(t, steps: int, warmup: int):
         sec = (time.perf_counter() - t0) / steps
         launches = (_native.launch_count() - l0) // steps
         got = tree.from_c(cs[-1])
+        # the device kernels of one more product, timed on their stream
+        extra = tree.to_c(t)
+        try:
+            _native.profile_start()
+            call(extra)
+            prof = _native.profile_stop()
+        finally:
+            tree.free_c(extra)
     finally:
         tree.free_c(ca)
         for c in cs:
@@ -610,8 +633,18 @@ def ppmm_workload(t, steps: int, warmup: int):
         "e2e": {"value": 1.0 / sec, "unit": "products/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "config": {"workload": _ppmm_workload_name(n, PPMM["leaf"], PPMM["rmax"], eps),
                    "ranks_in": tree.ranks_by_level(t), "ranks_out": tree.ranks_by_level(got),
-                   "stored_doubles_in": _stored(t), "stored_doubles_out": _stored(got)},
+                   "stored_doubles_in": _stored(t), "stored_doubles_out": _stored(got),
+                   "kernels_ms": {k: v[0] for k, v in prof.items()}},
     }
+    if prof:
+        # the dominant FP64 product kernel of one product against the run's DGEMM rate
+        name, (kms, kfl, _, _) = max(prof.items(), key=lambda kv: kv[1][0])
+        fp64 = fp64_gemm_peak()
+        ach = kfl / (kms / 1e3) / 1e12 if kms > 0 else 0.0
+        rec["roofline"] = {"kernel": f"{name} (FP64 apply kernels of the product)", "bound": "fp64", "achieved": ach,
+                           "peak": fp64["tflops"], "unit": "TFLOP/s", "frac": ach / fp64["tflops"], "traffic": None,
+                           "peak_source": "of " + fp64["source"],
+                           "note": "device kernels are part of the step; the rest moves the host trees"}
     return rec, got
 
 
