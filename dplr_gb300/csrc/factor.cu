@@ -191,10 +191,15 @@ __global__ void __launch_bounds__(256) lu_inverse_smem_kernel(double *base, cons
             for (int i = j + 1 + tid; i < n; i += bs) S[i + j * n] *= inv;
         }
         __syncthreads();
-        const int w = n - j - 1;
-        for (int e = tid; e < w * w; e += bs) {
-            const int i = j + 1 + e % w, c = j + 1 + e / w;
-            S[i + c * n] -= S[i + j * n] * S[j + c * n];
+        // trailing update: warps over columns, lanes over rows (no integer
+        // division per element); every element gets the same updates, in the
+        // same order, as in lu_inverse_kernel
+        {
+            const int lane = tid & 31, warp = tid >> 5, nwarp = bs >> 5;
+            for (int c = j + 1 + warp; c < n; c += nwarp) {
+                const double u = S[j + c * n];
+                for (int i = j + 1 + lane; i < n; i += 32) S[i + c * n] -= S[i + j * n] * u;
+            }
         }
         __syncthreads();
     }
