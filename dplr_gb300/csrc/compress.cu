@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -38,6 +39,7 @@
 #include "../../include/dplr_gb300.h"
 #include "gemm.cuh"
 #include "svdblock.cuh"
+#include "svdbatch.cuh"
 
 namespace dg {
 int fail(int code, const char *fmt, ...);
@@ -420,6 +422,105 @@ __global__ void scale_cols_kernel(double *__restrict__ u, const double *__restri
 }
 
 
+// The batched path (svdbatch.cuh) takes blocks of rank r <= min(n, limit)
+// with n r^2 <= 2^22, for which one CTA's QRs stay within milliseconds;
+// larger blocks go to the library workers below.  The limit is
+// kSvdBatchRank, or DPLR_GB300_SVD_BATCH_RANK from the environment (read on
+// every call; 0 sends every block to the library).
+int batch_rank_limit()
+{
+    const char *v = getenv("DPLR_GB300_SVD_BATCH_RANK");
+    if (!v || !*v) return dg::kSvdBatchRank;
+    return std::max(0, std::min(atoi(v), dg::kSvdBatchRank));
+}
+
+bool batch_takes(const dg::SvdBlock &b, int limit)
+{
+    return b.r > 0 && b.r <= limit && b.r <= b.n && (long long)b.n * b.r * b.r <= (1LL << 22);
+}
+
+// Truncated SVDs of blocks[ids[..]] by svd_batch_kernel, in launches of at
+// most 2^25 staged doubles.  res[id]: 0 done, 1 not converged (block left
+// as it was, rank = r); returns -1 on a CUDA error.
+int run_svd_batch(dg::SvdBlock *blocks, const std::vector<int> &ids, std::vector<int> &res)
+{
+    if (ids.empty()) return 0;
+    for (int id : ids) blocks[id].rank = blocks[id].r;
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return -1;
+    const long long cap = 1LL << 25;
+    bool ok = true;
+    for (size_t g0 = 0; ok && g0 < ids.size();) {
+        std::vector<dg::SvdBatchJob> jobs;
+        long long tot = 0;
+        int rmax = 0;
+        size_t g1 = g0;
+        for (; g1 < ids.size(); ++g1) {
+            const dg::SvdBlock &b = blocks[ids[g1]];
+            const long long need = (3LL * b.n * b.r + b.r + 3) & ~3LL;
+            if (!jobs.empty() && tot + need > cap) break;
+            jobs.push_back({tot, b.n, b.r, b.eps});
+            tot += need;
+            rmax = std::max(rmax, b.r);
+        }
+        const int cnt = (int)jobs.size();
+        double *stage = nullptr;
+        dg::SvdBatchJob *dj = nullptr;
+        int *dout = nullptr;
+        ok = cudaMalloc((void **)&stage, (size_t)tot * sizeof(double)) == cudaSuccess &&
+             cudaMalloc((void **)&dj, (size_t)cnt * sizeof(dg::SvdBatchJob)) == cudaSuccess &&
+             cudaMalloc((void **)&dout, (size_t)cnt * 2 * sizeof(int)) == cudaSuccess &&
+             cudaMemcpyAsync(dj, jobs.data(), (size_t)cnt * sizeof(dg::SvdBatchJob), cudaMemcpyHostToDevice, st) ==
+                 cudaSuccess;
+        for (int k = 0; ok && k < cnt; ++k) {
+            const dg::SvdBlock &b = blocks[ids[g0 + k]];
+            const size_t nr = (size_t)b.n * b.r;
+            double *u = stage + jobs[k].off;
+            ok = cudaMemcpyAsync(u, b.u, nr * sizeof(double), cudaMemcpyDefault, st) == cudaSuccess &&
+                 cudaMemcpyAsync(u + nr, b.v, nr * sizeof(double), cudaMemcpyDefault, st) == cudaSuccess &&
+                 cudaMemcpyAsync(u + 3 * nr, b.sig, (size_t)b.r * sizeof(double), cudaMemcpyDefault, st) ==
+                     cudaSuccess;
+        }
+        std::vector<int> hout((size_t)cnt * 2, 0);
+        if (ok) {
+            const int smem = dg::svd_batch_smem(rmax);
+            ok = cudaFuncSetAttribute(dg::svd_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ==
+                 cudaSuccess;
+            if (ok) {
+                dg::svd_batch_kernel<<<cnt, dg::kSvdThreads, smem, st>>>(dj, cnt, stage, dout);
+                dg::note_launch();
+                ok = cudaGetLastError() == cudaSuccess &&
+                     cudaMemcpyAsync(hout.data(), dout, (size_t)cnt * 2 * sizeof(int), cudaMemcpyDeviceToHost, st) ==
+                         cudaSuccess &&
+                     cudaStreamSynchronize(st) == cudaSuccess;
+            }
+        }
+        for (int k = 0; ok && k < cnt; ++k) {
+            dg::SvdBlock &b = blocks[ids[g0 + k]];
+            if (hout[2 * k + 1] != 0) {
+                res[ids[g0 + k]] = 1;
+                continue;
+            }
+            const int rank = std::min(std::max(hout[2 * k], 0), b.r);
+            const size_t nr = (size_t)b.n * b.r, nk = (size_t)b.n * rank;
+            const double *u = stage + jobs[k].off;
+            if (rank > 0)
+                ok = cudaMemcpyAsync(b.du, u, nk * sizeof(double), cudaMemcpyDefault, st) == cudaSuccess &&
+                     cudaMemcpyAsync(b.dv, u + 2 * nr, nk * sizeof(double), cudaMemcpyDefault, st) == cudaSuccess &&
+                     cudaMemcpyAsync(b.dsig, u + 3 * nr, (size_t)rank * sizeof(double), cudaMemcpyDefault, st) ==
+                         cudaSuccess;
+            b.rank = rank;
+        }
+        ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+        cudaFree(stage);
+        cudaFree(dj);
+        cudaFree(dout);
+        g0 = g1;
+    }
+    cudaStreamDestroy(st);
+    return ok ? 0 : -1;
+}
+
 // Buffers of one recompression worker, sized for the largest block.
 struct RWorker {
     cudaStream_t st = nullptr;
@@ -574,40 +675,50 @@ namespace dg {
 
 int svd_truncate_blocks(SvdBlock *blocks, int count, int workers)
 {
+    // small blocks: one batched launch; the others: the library workers
+    const int limit = batch_rank_limit();
+    std::vector<int> batched, order;
     int nmax = 0, rmax = 0;
-    for (int i = 0; i < count; ++i)
-        if (blocks[i].r > 0) {
+    for (int i = 0; i < count; ++i) {
+        blocks[i].rank = blocks[i].r;
+        if (blocks[i].r == 0 || blocks[i].n == 0) continue;
+        if (batch_takes(blocks[i], limit)) {
+            batched.push_back(i);
+        } else {
+            order.push_back(i);
             nmax = std::max(nmax, blocks[i].n);
             rmax = std::max(rmax, blocks[i].r);
         }
-    if (rmax == 0) {
-        for (int i = 0; i < count; ++i) blocks[i].rank = blocks[i].r;
-        return 0;
     }
-    if (!solver().ok) return report(DPLR_GPU_ECUDA, "SVD recompression: cannot load cuSOLVER (libcusolver.so.12)");
-    std::vector<int> order(count);
-    for (int i = 0; i < count; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return (long long)blocks[a].n * blocks[a].r > (long long)blocks[b].n * blocks[b].r;
-    });
-    int nw = workers > 0 ? workers : 8;
-    nw = std::max(1, std::min(nw, count));
-    std::vector<RWorker> pool(nw);
-    bool ok = true;
-    for (RWorker &w : pool) ok = ok && w.init(nmax, rmax);
     std::vector<int> res(count, 0);
-    if (ok) {
-        std::atomic<int> next{0};
-        auto body = [&](RWorker &w) {
-            for (int k = next.fetch_add(1); k < count; k = next.fetch_add(1)) res[order[k]] = w.run(blocks[order[k]]);
-        };
-        std::vector<std::thread> th;
-        for (int t = 1; t < nw; ++t) th.emplace_back(body, std::ref(pool[t]));
-        body(pool[0]);
-        for (std::thread &t : th) t.join();
+    if (run_svd_batch(blocks, batched, res) < 0)
+        return report(DPLR_GPU_ECUDA, "SVD recompression: CUDA call of the batched SVD failed");
+    const int nbig = (int)order.size();
+    if (nbig > 0) {
+        if (!solver().ok)
+            return report(DPLR_GPU_ECUDA, "SVD recompression: cannot load cuSOLVER (libcusolver.so.12)");
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return (long long)blocks[a].n * blocks[a].r > (long long)blocks[b].n * blocks[b].r;
+        });
+        int nw = workers > 0 ? workers : 8;
+        nw = std::max(1, std::min(nw, nbig));
+        std::vector<RWorker> pool(nw);
+        bool ok = true;
+        for (RWorker &w : pool) ok = ok && w.init(nmax, rmax);
+        if (ok) {
+            std::atomic<int> next{0};
+            auto body = [&](RWorker &w) {
+                for (int k = next.fetch_add(1); k < nbig; k = next.fetch_add(1))
+                    res[order[k]] = w.run(blocks[order[k]]);
+            };
+            std::vector<std::thread> th;
+            for (int t = 1; t < nw; ++t) th.emplace_back(body, std::ref(pool[t]));
+            body(pool[0]);
+            for (std::thread &t : th) t.join();
+        }
+        for (RWorker &w : pool) w.release();
+        if (!ok) return report(DPLR_GPU_ECUDA, "SVD recompression: device setup failed");
     }
-    for (RWorker &w : pool) w.release();
-    if (!ok) return report(DPLR_GPU_ECUDA, "SVD recompression: device setup failed");
     for (int r : res)
         if (r < 0) return report(DPLR_GPU_ECUDA, "SVD recompression: CUDA or cuSOLVER call failed");
     for (int r : res)

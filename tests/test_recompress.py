@@ -125,6 +125,52 @@ def test_gpu_bounds_the_rank_growth_of_a_product():
 
 
 @pytest.mark.gpu
+def test_batched_kernel_matches_the_library_path(monkeypatch):
+    """Blocks of rank <= 64 take the batched kernel (Householder QR and
+    one-sided Jacobi in one CTA per block), larger ones the library SVD.
+    A tree with both: the result matches the restatement either way, and
+    with DPLR_GB300_SVD_BATCH_RANK=0 (every block on the library) too; the
+    kept columns are orthonormal."""
+    t = _doubled(gen.random_tree(1024, 64, [40, 24, 12, 6], seed=6, diag_shift=2.0, decay=0.7))
+    assert t.ne.rank == 80 and t.nw.ne.rank == 48        # library and batched blocks
+    eps = 1e-6
+    want = orec.reduce_svd(t, eps)
+    got = _gpu(t, eps)
+    assert_same_blocks(got, want, tol=1e-12)
+    for g, _ in _blocks(got, eps=1.0):
+        if g.rank:
+            k = np.eye(g.rank)
+            assert np.abs(g.u.T @ g.u - k).max() <= 1e-12
+            assert np.abs(g.v.T @ g.v - k).max() <= 1e-12
+    monkeypatch.setenv("DPLR_GB300_SVD_BATCH_RANK", "0")
+    assert_same_blocks(_gpu(t, eps), want, tol=1e-12)
+
+
+@pytest.mark.gpu
+def test_batched_kernel_on_tall_repeated_and_zero_blocks():
+    """The batched kernel at its edges: 2048 rows with every column
+    repeated (the copies' reflectors fall below rounding and are skipped),
+    a block whose sig are all zero, and eps = 0 (every singular value
+    kept, the product unchanged)."""
+    rng = np.random.default_rng(12)
+    n = 2048
+    u, v = rng.standard_normal((n, 8)), rng.standard_normal((n, 8))
+    s = np.abs(rng.standard_normal(8)) + 0.5
+    tall = tree.LowRank(np.hstack([u, u]), np.concatenate([s, s]), np.hstack([v, v]), capacity=18)
+    zero = tree.LowRank(rng.standard_normal((n, 5)), np.zeros(5), rng.standard_normal((n, 5)), capacity=5)
+    t = tree.HNode(tree.Dense(rng.standard_normal((n, n))), tall, tree.Dense(rng.standard_normal((n, n))), zero)
+    got = _gpu(t, 1e-8)
+    assert got.ne.rank == 8 and got.sw.rank == 0
+    assert_same_blocks(got, orec.reduce_svd(t, 1e-8), tol=1e-12)
+    small = _doubled(gen.random_tree(256, 32, [6, 4, 3], seed=9, diag_shift=2.0))
+    got0 = _gpu(small, 0.0)
+    for (g, _), (w, _) in zip(_blocks(got0, eps=1.0), _blocks(small, eps=1.0)):
+        assert g.rank == w.rank
+    dense = tree.to_dense(small)
+    assert np.abs(tree.to_dense(got0) - dense).max() <= 1e-12 * np.abs(dense).max()
+
+
+@pytest.mark.gpu
 def test_gpu_rejects_invalid_arguments():
     from dplr_gb300 import _native
     lib = _native.lib()
