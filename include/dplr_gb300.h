@@ -319,8 +319,13 @@ DPLR_API void dplr_gpu_release_staging(void);
  * becomes its truncated SVD (QR of U diag(s) and of V, SVD of Ru Rv^T on
  * the GPU), keeping the singular values >= the block's threshold, eps/4
  * per level as dplrreduce splits it.  Ranks only shrink, capacities stay.
- * workers: host threads with their own stream and cuSOLVER handle (0 = 8).
- * DPLR_GPU_ENOTCONV if an SVD did not converge (that block is kept). */
+ * Blocks of rank r <= min(n, 64) with n r^2 <= 2^22 run together in one
+ * launch of the library's own kernel (Householder QR and one-sided Jacobi,
+ * one CTA per block); DPLR_GB300_SVD_BATCH_RANK in the environment (0..64,
+ * read on every call) lowers that rank limit.  The other blocks use
+ * cuSOLVER on `workers` host threads, each with its own stream and handle
+ * (0 = 8).  DPLR_GPU_ENOTCONV if an SVD did not converge (that block is
+ * kept). */
 DPLR_API int dplr_gpu_reduce_svd(int m, DPlrMtx *A, double eps, int workers);
 
 /* Associate the drop-in entry points with a plan for this host tree
