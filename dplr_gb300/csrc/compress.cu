@@ -398,6 +398,95 @@ struct Worker {
 
 const char *block_name(const Job &jb) { return jb.r0 < jb.c0 ? "NE" : "SW"; }
 
+// Staging of dense blocks for svd_batch_kernel: V = I and sig = 1 (the
+// block itself is copied into U), one CTA per block.
+__global__ void svd_stage_dense_kernel(const dg::SvdBatchJob *__restrict__ jobs, int count, double *__restrict__ stage)
+{
+    if ((int)blockIdx.x >= count) return;
+    const dg::SvdBatchJob jb = jobs[blockIdx.x];
+    const long long nn = (long long)jb.n * jb.n;
+    double *v = stage + jb.off + nn, *sig = v + 2 * nn;
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) v[e] = (e % jb.n) == (e / jb.n) ? 1.0 : 0.0;
+    for (int e = threadIdx.x; e < jb.n; e += blockDim.x) sig[e] = 1.0;
+}
+
+// Truncated SVDs of the blocks of order n <= the batched kernel's rank limit
+// (dplrlrappx, src/dplrd2p.c:22) in one launch: each block is the rank-n
+// product A I^T.  rc[order]: 0, 1 (the Jacobi sweeps did not converge,
+// devinfo 1); returns -1 on a CUDA error.
+int run_dense_batch(const double *dA, int m, std::vector<Job> &jobs, const std::vector<int> &ids, std::vector<int> &rc)
+{
+    if (ids.empty()) return 0;
+    std::vector<dg::SvdBatchJob> bj;
+    long long tot = 0;
+    int nmax = 0;
+    for (int id : ids) {
+        const Job &jb = jobs[id];
+        bj.push_back({tot, jb.n, jb.n, jb.eps});
+        tot += (3LL * jb.n * jb.n + jb.n + 3) & ~3LL;
+        nmax = std::max(nmax, jb.n);
+    }
+    const int cnt = (int)bj.size();
+    cudaStream_t st = nullptr;
+    double *stage = nullptr;
+    dg::SvdBatchJob *dj = nullptr;
+    int *dout = nullptr;
+    std::vector<int> hout((size_t)cnt * 2, 0);
+    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc((void **)&stage, (size_t)tot * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void **)&dj, (size_t)cnt * sizeof(dg::SvdBatchJob)) == cudaSuccess &&
+              cudaMalloc((void **)&dout, (size_t)cnt * 2 * sizeof(int)) == cudaSuccess &&
+              cudaMemcpyAsync(dj, bj.data(), (size_t)cnt * sizeof(dg::SvdBatchJob), cudaMemcpyHostToDevice, st) ==
+                  cudaSuccess;
+    for (int k = 0; ok && k < cnt; ++k) {
+        const Job &jb = jobs[ids[k]];
+        ok = cudaMemcpy2DAsync(stage + bj[k].off, (size_t)jb.n * sizeof(double), dA + jb.r0 + (size_t)jb.c0 * m,
+                               (size_t)m * sizeof(double), (size_t)jb.n * sizeof(double), jb.n,
+                               cudaMemcpyDeviceToDevice, st) == cudaSuccess;
+    }
+    if (ok) {
+        svd_stage_dense_kernel<<<cnt, 256, 0, st>>>(dj, cnt, stage);
+        dg::note_launch();
+        const int smem = dg::svd_batch_smem(nmax);
+        ok = cudaGetLastError() == cudaSuccess &&
+             cudaFuncSetAttribute(dg::svd_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ==
+                 cudaSuccess;
+        if (ok) {
+            dg::svd_batch_kernel<<<cnt, dg::kSvdThreads, smem, st>>>(dj, cnt, stage, dout);
+            dg::note_launch();
+            ok = cudaGetLastError() == cudaSuccess &&
+                 cudaMemcpyAsync(hout.data(), dout, (size_t)cnt * 2 * sizeof(int), cudaMemcpyDeviceToHost, st) ==
+                     cudaSuccess &&
+                 cudaStreamSynchronize(st) == cudaSuccess;
+        }
+    }
+    for (int k = 0; ok && k < cnt; ++k) {
+        Job &jb = jobs[ids[k]];
+        DPlrMtx *L = jb.L;
+        if (hout[2 * k + 1] != 0) {
+            jb.devinfo = 1;
+            rc[jb.order] = 1;
+            continue;
+        }
+        const int n = jb.n, rank = std::min(std::max(hout[2 * k], 0), n);
+        if (L->dlr.capacity < rank) dplrresizelr(L, rank);
+        L->dlr.rank = rank;
+        if (rank == 0) continue;
+        const double *u = stage + bj[k].off;
+        const size_t nn = (size_t)n * n, nk = (size_t)n * rank;
+        ok = cudaMemcpyAsync(L->dlr.u, u, nk * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaMemcpyAsync(L->dlr.v, u + 2 * nn, nk * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaMemcpyAsync(L->dlr.sig, u + 3 * nn, (size_t)rank * sizeof(double), cudaMemcpyDeviceToHost, st) ==
+                 cudaSuccess;
+    }
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    cudaFree(stage);
+    cudaFree(dj);
+    cudaFree(dout);
+    if (st) cudaStreamDestroy(st);
+    return ok ? 0 : -1;
+}
+
 // ------------------------------------------------ SVD-based recompression
 
 // R (k x r, ld k) = the upper triangle of the first k rows of a geqrf result
@@ -760,14 +849,20 @@ int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int 
             fprintf(stderr, "dplrd2gep: failed to approximate %s block\n", block_name(jb));
             return DPLR_GPU_OK;
         }
-    if (!solver().ok)
+    // blocks of order <= the batched kernel's limit run together on it; the
+    // others on the library workers
+    const int limit = batch_rank_limit();
+    std::vector<int> batched, big;
+    for (size_t i = 0; i < jobs.size(); ++i) (jobs[i].n > 0 && jobs[i].n <= limit ? batched : big).push_back((int)i);
+    if (!big.empty() && !solver().ok)
         return report(DPLR_GPU_ECUDA, "dplrd2gep: cannot load cuSOLVER (libcusolver.so.12)");
 
     // device copy of A, ld m
     double *dA = nullptr;
     if (cudaMalloc((void **)&dA, (size_t)m * m * sizeof(double)) != cudaSuccess ||
         cudaMemcpy2D(dA, (size_t)m * sizeof(double), A, (size_t)lda * sizeof(double), (size_t)m * sizeof(double), m,
-                     cudaMemcpyHostToDevice) != cudaSuccess) {
+                     cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaStreamSynchronize(nullptr) != cudaSuccess) {   // the blocks read dA on streams of their own
         cudaFree(dA);
         return report(DPLR_GPU_ECUDA, "dplrd2gep: device copy of A failed");
     }
@@ -779,17 +874,21 @@ int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int 
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     int nw = workers > 0 ? workers : 8;
-    nw = std::min<int>(nw, (int)jobs.size());
-    nw = (int)std::max<size_t>(1, std::min<size_t>((size_t)nw, fr / 4 / std::max<size_t>(per, 1)));
+    nw = std::min<int>(nw, (int)big.size());
+    nw = big.empty() ? 0 : (int)std::max<size_t>(1, std::min<size_t>((size_t)nw, fr / 4 / std::max<size_t>(per, 1)));
     std::vector<Worker> pool(nw);
     bool ok = true;
     for (Worker &w : pool) ok = ok && w.init(nmax);
 
     std::vector<int> rc(jobs.size(), 0);
-    if (ok) {
+    if (ok && run_dense_batch(dA, m, jobs, batched, rc) < 0) {
+        for (Worker &w : pool) w.release();
+        cudaFree(dA);
+        return report(DPLR_GPU_ECUDA, "dplrd2gep: CUDA call of the batched SVD failed");
+    }
+    if (ok && !big.empty()) {
         // largest blocks first; ties in DPLR's order
-        std::vector<int> idx(jobs.size());
-        for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+        std::vector<int> idx(big);
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return jobs[a].n > jobs[b].n; });
         std::atomic<int> next{0};
         std::atomic<bool> failed{false};

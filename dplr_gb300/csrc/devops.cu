@@ -219,6 +219,7 @@ int plan_reduce(Plan *p, double eps, int workers, cudaStream_t st, Plan **out)
     DG_ALLOC(&scratch, bytes);
     // a block whose SVD does not converge keeps its factors: start from a copy
     cudaError_t e = cudaMemcpy(scratch, p->pool, bytes, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);   // done before other streams write the scratch
     if (e != cudaSuccess) {
         cudaFree(scratch);
         return fail(DPLR_GPU_ECUDA, "plan recompression: %s", cudaGetErrorString(e));
