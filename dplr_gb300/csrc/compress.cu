@@ -10,8 +10,11 @@
 //     and eps/4 otherwise, passed down to the diagonal blocks.
 // B is reshaped first, with DPLR's rule (a node whose type or size differs
 // is cleared and rebuilt), and every off-diagonal block becomes one SVD job.
-// A is copied to the device once; the jobs, largest first, are spread over
-// worker threads, each with its own stream, cuSOLVER handle and buffers:
+// A is copied to the device once.  Blocks of up to 64 rows run together in
+// one launch of the batched SVD kernel (svdbatch.cuh: Householder QR and
+// one-sided Jacobi, one CTA per block).  The other jobs, largest first,
+// are spread over worker threads, each with its own stream, cuSOLVER
+// handle and buffers:
 // the SVD (cuSOLVER's gesvd, the QR-iteration SVD LAPACK's dgesvd is) of a
 // small block is a long chain of small launches, so independent blocks run
 // side by side.  Blocks of 512 and more first try a sketch: Q = orth(A
@@ -21,8 +24,11 @@
 // accurate as a full SVD's, the SVD of the n x l matrix B^T gives the
 // block's factors, otherwise the full SVD runs.  The tree B stays on the
 // host, as DPLR's callers expect.
+// The SVD-based recompression (dplr_gpu_reduce_svd) shares the batched
+// kernel for its blocks of rank <= 64 and the library for the others.
 // Argument checks, messages and info codes are DPLR's: info = -1 on invalid
-// arguments, the SVD's info if one does not converge.
+// arguments, the SVD's info if one does not converge (1 for the batched
+// kernel).
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 #include <dlfcn.h>

@@ -298,7 +298,10 @@ DPLR_API int dplr_gpu_profile_entry(int i, const char **name, double *ms, double
 
 /* dplrd2gep with the number of SVD workers chosen (each a host thread with
  * its own stream, cuSOLVER handle and buffers; 0 = 8, fewer where device
- * memory is short).  dplrd2gep is this call with workers = 0.  Returns
+ * memory is short).  Blocks of up to 64 rows (DPLR_GB300_SVD_BATCH_RANK
+ * lowers the limit) run together in one launch of the library's own SVD
+ * kernel instead; a block whose Jacobi sweeps do not converge gives info 1.
+ * dplrd2gep is this call with workers = 0.  Returns
  * DPLR_GPU_EINVAL on invalid arguments, DPLR_GPU_ECUDA on a CUDA or
  * cuSOLVER error, else DPLR_GPU_OK with DPLR's info in *info. */
 DPLR_API int dplr_gpu_d2gep(int m, const double *A, int lda, DPlrMtx *B, double eps, int nlvl,

@@ -3,7 +3,8 @@
 The golden fixtures exp256 and invdist256 hold trees that the reference's
 own dplrd2gep made from dense inputs rebuilt here: the numpy restatement
 (gen.compress_dense) is pinned against them on the CPU, and the GPU
-library's dplrd2gep (SVDs by cuSOLVER) is held to the same trees and to the
+library's dplrd2gep (SVDs by its own batched kernel up to 64 rows, by
+cuSOLVER above) is held to the same trees and to the
 restatement on larger inputs.  Singular vectors are compared through the
 blocks they build (their signs are the SVD's choice); ranks must be equal.
 """
